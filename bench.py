@@ -1,0 +1,290 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 qMC diagram-integration path.
+
+A step is one regular inch step of `inchworm!` (src/inchworm.jl:474-493) on the two-orbital
+eg Kanamori model with a discrete bath (beta = 8, n_tau = 256, orders 0:4, N_samples = 2^10
+unscrambled Sobol points per topology group): all 16 sampled topology groups of the step in
+one launch, the exact order-0 term, then set_ppgf!/normalize! on the host.  The metric is
+topology-sample evaluations per second ("diagram evals/s": one (topology, qMC point) pair,
+the unit of src/topology_eval.jl:392).
+
+  value    device-resident throughput: kernel time (CUDA events on the library's stream).
+  e2e      the same through the C ABI with host buffers: P upload, launch, result download
+           and the host-side P update are inside the timed region.
+  --impl reference  times the reference's algorithm on the host cores: the CPU oracle (a C
+           restatement of src/topology_eval.jl; Julia and QInchworm.jl are not available),
+           threaded over sample ranges like MPI ranks, on a bounded sample of the same step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "qinchworm.jl_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "diagram evals/s (topology-sample evaluations per second), plain FP64 inch step"
+UNIT = "topology-samples/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--samples", type=int, default=1024)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--model", default="eg", choices=["eg", "anderson"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(model: str):
+    from qiw import models
+    if model == "eg":
+        return models.eg_discrete_bath(n_tau=256), "eg Kanamori U=2 J=0.2 beta=8 n_tau=256, 4-level bath"
+    return models.anderson(n_tau=200), "Anderson eps=0.1 U=1 beta=10 n_tau=200, semi-elliptic bath"
+
+
+def bold_groups(orders, N):
+    from qiw.diagrammatics import get_topologies_at_order
+    from qiw.inchworm import TopologiesInputData
+    tds = []
+    for o in orders:
+        for npa in ([0] if o == 0 else range(1, 2 * o)):
+            tops = get_topologies_at_order(o, npa)
+            if tops:
+                tds.append(TopologiesInputData(o, npa, tops, N))
+    return tds
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons)}
+
+
+def fp64_peak_tflops() -> float:
+    """Measured FP64 rate of this GPU: cuBLAS DGEMM 4096^3, best of 3 (CUDA events)."""
+    import torch
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * 4096 ** 3 / best / 1e12
+
+
+def cpu_baseline(exp, tds, samples_cap: int, budget_s: float = 15.0):
+    """Oracle (C restatement of the reference evaluator) on one inch step, all host cores,
+    bounded number of samples per group; returns (topology-samples/s, cores, description)."""
+    import oracle as orc
+    cores = os.cpu_count() or 1
+    pb = orc.OracleProblem(exp)
+    g = exp.grid
+    n = g.n_tau // 2
+    t = (g.tau(0), g.tau(n), g.tau(n + 1))
+    # calibrate on the heaviest group
+    heavy = max(tds, key=lambda td: (td.order, len(td.topologies)))
+    n_try = max(cores, 16)
+    t0 = time.perf_counter()
+    pb.integrate("bold", heavy.order, heavy.n_pts_after, [(x.pairs, x.parity) for x in heavy.topologies], *t,
+                 n_try, n_ranks=cores)
+    dt = time.perf_counter() - t0
+    per_sample_heavy = dt / n_try
+    est = sum(per_sample_heavy * len(td.topologies) / len(heavy.topologies) for td in tds if td.order > 0)
+    N = int(max(cores, min(samples_cap, budget_s / max(est, 1e-9))))
+    t0 = time.perf_counter()
+    units = 0
+    for td in tds:
+        if td.order == 0:
+            continue
+        pb.integrate("bold", td.order, td.n_pts_after, [(x.pairs, x.parity) for x in td.topologies], *t, N,
+                     n_ranks=cores)
+        units += len(td.topologies) * N
+    el = time.perf_counter() - t0
+    return units / el, cores, f"one inch step (tau_w index {n}), {N} Sobol samples per group, {len(tds)} groups"
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    exp, desc = workload(args.model)
+    tds = bold_groups(range(0, 5), args.samples)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, cores, sample = cpu_baseline(exp, tds, args.samples, budget_s=8.0)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": desc + ", orders 0:4, one inch step", "N_samples": args.samples},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    from qiw import _lib, ppgf
+    from qiw.device import Device
+    from qiw.inchworm import _Session, _accumulate, Comm, TorchComm
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    comm = Comm()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        comm = TorchComm()
+    torch.cuda.set_device(local)
+    prec = _lib.QIW_PREC_FP32 if args.precision == "fp32" else _lib.QIW_PREC_FP64
+    exp, desc = workload(args.model)
+    grid = exp.grid
+    # weak scaling: every rank evaluates N_samples per group; the step result is all-reduced
+    N = args.samples
+    tds = bold_groups(range(0, 5), N * world)
+    dev = Device(local)
+    ses = _Session(dev, exp)
+    for td in tds:
+        ses.group(_lib.QIW_GROUP_BOLD, td)
+    stats = {id(td): dev.group_stats(ses.group(_lib.QIW_GROUP_BOLD, td)) for td in tds}
+    units_rank = sum(len(td.topologies) * (N if td.order > 0 else 1) for td in tds if td.order > 0)
+    flops_rank = sum(stats[id(td)].flops_per_sample * N for td in tds if td.order > 0)
+    # bare step, then warm-up and timed regular steps
+    from qiw.inchworm import TopologiesInputData
+    from qiw.diagrammatics import get_topologies_at_order
+    bare = [TopologiesInputData(o, 2 * o, get_topologies_at_order(o), N * world) for o in range(0, 5)]
+    val, _, _ = _accumulate(ses.run(_lib.QIW_GROUP_BARE, bare, grid.tau(0), 0.0, grid.tau(1), prec, comm), bare,
+                            exp.dims)
+    ppgf.set_ppgf(exp.P, 1, val)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    kernel_ms, wall_s = [], []
+    h2d = d2h = 0
+
+    def step(n):
+        dev.set_ppgf(exp.P)
+        res = ses.run(_lib.QIW_GROUP_BOLD, tds, grid.tau(0), grid.tau(n), grid.tau(n + 1), prec, comm)
+        v, _, _ = _accumulate(res, tds, exp.dims)
+        ppgf.set_ppgf(exp.P, n + 1, v)
+        ppgf.normalize_tau(exp.P, n + 1)
+
+    n = 1
+    for _ in range(args.warmup):
+        step(n)
+        n += 1
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    for _ in range(args.steps):
+        flush.fill_(float(n))  # write 256 MB (> L2) between timed steps
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step(n)
+        wall_s.append(time.perf_counter() - t0)
+        kernel_ms.append(dev.last_kernel_ms())
+        n += 1
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = clk.stop()
+    k_tot = sum(kernel_ms) / 1e3
+    w_tot = sum(wall_s)
+    if world > 1:
+        t = torch.tensor([k_tot, w_tot], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        k_tot, w_tot = float(t[0]), float(t[1])
+    units = units_rank * world * args.steps
+    # bytes copied per step: i*P tables (FP64 + FP32), work/Sobol descriptors; results back
+    S2 = int(np.sum(np.array(exp.dims) ** 2))
+    h2d = grid.n_tau * S2 * (8 + 4) + len(tds) * (80 + 4 * 32 * 8 + 16)
+    d2h = len(tds) * S2 * 16 + 4
+    if rank != 0:
+        return
+    peak = fp64_peak_tflops() if args.precision == "fp64" else None
+    achieved = flops_rank * args.steps / k_tot / 1e12
+    line = {
+        "metric": METRIC if args.precision == "fp64" else METRIC.replace("plain FP64", "FP32 chain products"),
+        "value": units / k_tot, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * k_tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64acc", "data": "synthetic",
+        "config": {"workload": desc + ", orders 0:4, one regular inch step per bench step",
+                   "N_samples": N * world, "groups_per_step": len(tds),
+                   "topologies_per_step": sum(len(td.topologies) for td in tds), "l2": "256 MB write between timed steps"},
+        "e2e": {"value": units / w_tot, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": 1e3 * w_tot / args.steps},
+        "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": (achieved / peak) if peak else None, "traffic": None,
+                     "peak_source": "measured cuBLAS DGEMM 4096^3 on this GPU (no FP64 entry in MEASURED_PEAKS.json)",
+                     "flops_per_step": flops_rank},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        v, cores, sample = cpu_baseline(exp, tds, N)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

@@ -1,0 +1,146 @@
+/*
+ * qiw -- GB300-native qMC diagram integration for the inchworm algorithm (C ABI).
+ *
+ * One library call replaces the per-(inch step, topology group) qMC integral that
+ * QInchworm.jl evaluates with
+ *     contour_integral(t -> eval(td.topologies, t), c, trans; seq, N)
+ * at src/inchworm.jl:181-187 (bold step), :281-287 (bare step) and :868-875 (correlator),
+ * i.e. the value `res` just before `all_reduce!` (src/inchworm.jl:178-189):
+ *     res = rank_weight * (1/N_rank) * sum_{i in rank range} prod(branch_direction) * J * eval(u(x_i)).
+ *
+ * Conventions
+ *   - All pointers are host pointers owned by the caller for the duration of the call;
+ *     calls are synchronous (results are in the output buffers on return).
+ *   - Complex numbers are interleaved (re, im) doubles, exactly Julia's ComplexF64 layout.
+ *   - Matrices are column-major (Julia's Matrix layout); sectors are 0-based.
+ *   - Every entry point returns QIW_OK (0) or an error code; qiw_last_error() gives text.
+ *     Nothing aborts the process.
+ *   - One context per host thread; a context owns its device buffers and CUDA stream.
+ */
+#ifndef QIW_H
+#define QIW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QIW_OK 0
+#define QIW_ERR_ARG 1          /* invalid argument / layout */
+#define QIW_ERR_CUDA 2         /* CUDA runtime failure */
+#define QIW_ERR_UNSUPPORTED 3  /* valid input outside what this build supports */
+#define QIW_ERR_OFFDIAG 4      /* block off-diagonal leaf (src/topology_eval.jl:462-464) */
+#define QIW_ERR_DEVICE 5       /* kernel error word set (bounds / non-finite result) */
+#define QIW_ERR_MEMORY 6       /* plan exceeds the per-sample working-set budget */
+
+/* propagator (Delta) interpolation rules */
+#define QIW_PROP_LINEAR 0      /* Keldysh ImaginaryTimeGF call (linear on the grid) */
+#define QIW_PROP_CUBIC 1       /* SplineInterpolatedGF: natural cubic spline (src/spline_gf.jl:195-202) */
+
+/* topology group kinds (fixed-node layouts of src/inchworm.jl) */
+#define QIW_GROUP_BOLD 0       /* IdentityNode(t_i), InchNode(t_w), IdentityNode(t_f); P bold  (:161-165) */
+#define QIW_GROUP_BARE 1       /* IdentityNode(t_i), IdentityNode(t_f); exact atomic P0         (:266-268) */
+#define QIW_GROUP_CORRELATOR 2 /* OperatorNode(B,t_i), OperatorNode(A,t_w), IdentityNode(t_f)  (:846-850) */
+
+/* arithmetic of the chain products */
+#define QIW_PREC_FP64 0        /* plain FP64 throughout */
+#define QIW_PREC_FP32 1        /* FP32 chain products, FP64 compensated accumulation of qMC sums */
+
+typedef struct qiw_ctx qiw_ctx;
+
+/* Replaces: nothing in the reference (it has no device state); creates a context on a device. */
+int qiw_ctx_create(qiw_ctx **out, int device);
+void qiw_ctx_destroy(qiw_ctx *ctx);
+/* Last error message of this context (never NULL). */
+const char *qiw_last_error(const qiw_ctx *ctx);
+
+/*
+ * Problem data of an `Expansion` (src/expansion.jl:107-197).
+ * Operators are SectorBlockMatrix objects (src/sector_block_matrix.jl:44): operator o has
+ * op_n_blocks[o] blocks; block b of it is (s_i, s_f) = op_blocks[2*k], op_blocks[2*k+1]
+ * (k = running block index over all operators) with a d_f x d_i column-major complex
+ * matrix at op_values + 2*op_value_offset[k].
+ */
+typedef struct {
+    int32_t n_sectors;
+    const int32_t *sector_dims;        /* [n_sectors] */
+    double beta;
+    int32_t n_tau;                     /* uniform grid tau_j = j*beta/(n_tau-1) */
+    const double *atomic_energies;     /* [sum d]: E + lambda of ExactAtomicPPGF (src/exact_atomic_ppgf.jl:134) */
+    int32_t n_ops;
+    const int32_t *op_n_blocks;        /* [n_ops] */
+    const int32_t *op_blocks;          /* [2 * total blocks] */
+    const int64_t *op_value_offset;    /* [total blocks], in complex elements */
+    const double *op_values;           /* complex */
+    int32_t identity_op;               /* index of expansion.identity_mat */
+    int32_t n_pairs;                   /* InteractionPair list (src/expansion.jl:79-90) */
+    const int32_t *pair_ops;           /* [2*n_pairs]: (operator_i, operator_f) operator indices */
+    const int32_t *pair_prop_kind;     /* [n_pairs]: QIW_PROP_* */
+    const double *pair_prop_data;      /* [n_pairs][n_tau] complex: propagator(tau_j, 0) */
+} qiw_problem_desc;
+
+/* Replaces: the per-call reads of expansion.P0/pairs/operators in TopologyEvaluator
+ * (src/topology_eval.jl:249-331).  Invalidates previously created groups. */
+int qiw_problem_set(qiw_ctx *ctx, const qiw_problem_desc *desc);
+
+/* Replaces: the bold P read by kd.interpolate! (src/topology_eval.jl:368) after
+ * set_ppgf!/normalize! (src/inchworm.jl:487-488).  `P` holds, for each sector s in
+ * order, expansion.P[s].mat.data: d_s x d_s x n_tau complex, column-major. */
+int qiw_ppgf_set(qiw_ctx *ctx, const double *P);
+
+/* A TopologiesInputData group (src/inchworm.jl:76-87). */
+typedef struct {
+    int32_t kind;                      /* QIW_GROUP_* */
+    int32_t order;
+    int32_t n_pts_after;               /* d_after; ignored for QIW_GROUP_BARE */
+    int32_t corr_A_op, corr_B_op;      /* QIW_GROUP_CORRELATOR: operator indices of A and B */
+    int32_t n_topologies;
+    const int32_t *top_pairs;          /* [n_topologies][order][2]: Topology.pairs (1-based vertices) */
+    const int32_t *top_parity;         /* [n_topologies]: Topology.parity */
+} qiw_group_desc;
+
+/* Replaces: TopologyEvaluator construction (src/topology_eval.jl:249-331).  Plans the
+ * group: the configuration tree of every topology and initial sector is enumerated once
+ * (it does not depend on the sample times) and configurations that share their future
+ * are merged; the result is a sample-independent instruction stream. */
+int qiw_group_create(qiw_ctx *ctx, const qiw_group_desc *desc, int32_t *group_id);
+
+typedef struct {
+    int64_t n_nodes_dag;       /* merged configuration-DAG states */
+    int64_t n_instructions;
+    int64_t arena_elements;    /* per-sample working set (matrix elements) */
+    double flops_per_sample;   /* algorithmic flops executed per qMC sample */
+    double tree_flops_per_sample; /* flops the reference's per-topology tree would need */
+    int64_t n_leaves_tree;     /* configurations the reference traverses per sample */
+} qiw_group_stats;
+
+int qiw_group_stats_get(qiw_ctx *ctx, int32_t group_id, qiw_group_stats *out);
+
+/* One qMC integral of one group over a contiguous Sobol index range. */
+typedef struct {
+    int32_t group;
+    int32_t reserved;
+    double t_i, t_w, t_f;              /* t_w unused for QIW_GROUP_BARE */
+    uint64_t first_index;              /* 0-based Sobol point index = first(N_range) - 1 */
+    uint64_t n_samples;                /* length(N_range) */
+    uint64_t n_total;                  /* td.N_samples (rank_weight = n_samples / n_total) */
+    const uint32_t *sobol_m;           /* [2*order][32] direction numbers (ScrambledSobolSeq.m, row d) */
+    const uint32_t *sobol_x0;          /* [2*order] initial point (digital shift; zeros if unscrambled) */
+} qiw_work_desc;
+
+/* Replaces: contour_integral(...) for each work item (src/qmc_integrate.jl:597-612 with the
+ * integrand of src/topology_eval.jl:350-437).  out: for each work item, the result
+ * SectorBlockMatrix as sum_s d_s^2 complex values (sector s block, column-major, sectors
+ * in order).  All work items run in one launch. */
+int qiw_integrate(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, int32_t precision,
+                  double *out);
+
+/* Kernel time of the most recent qiw_integrate (ms, CUDA events on the context stream). */
+double qiw_last_kernel_ms(const qiw_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QIW_H */

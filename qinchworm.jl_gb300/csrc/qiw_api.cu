@@ -1,0 +1,508 @@
+// C-ABI implementation: contexts, problem upload, group planning, integration calls.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "qiw.h"
+#include "qiw_internal.hpp"
+#include "qiw_kernels.hpp"
+#include "qiw_plan.hpp"
+
+using namespace qiw;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t reserve(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    size_t c = std::max<size_t>(count, 1);
+    cudaError_t e = cudaMalloc(&p, c * sizeof(T));
+    if (e == cudaSuccess) n = c;
+    return e;
+  }
+  cudaError_t upload(const T *h, size_t count, cudaStream_t s) {
+    cudaError_t e = reserve(count);
+    if (e != cudaSuccess || count == 0) return e;
+    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
+  }
+};
+
+struct GroupRec {
+  Plan plan;
+  DevBuf<PmJob> pm;
+  DevBuf<WJob> wj;
+  DevBuf<Instr> ins;
+  DevGroup dg;
+};
+
+// Natural cubic spline of y on a uniform grid; per segment a0 + a1 f + a2 f^2 + a3 f^3.
+void cubic_coeffs(const std::vector<double> &y, double h, std::vector<double> *out) {
+  const int n = (int)y.size();
+  std::vector<double> M(n, 0.0);
+  if (n >= 3) {
+    const int m = n - 2;
+    std::vector<double> cp(m), dp(m);
+    for (int i = 0; i < m; ++i) {
+      double rhs = 6.0 * (y[i + 2] - 2.0 * y[i + 1] + y[i]) / (h * h);
+      double den = (i == 0) ? 4.0 : 4.0 - cp[i - 1];
+      cp[i] = 1.0 / den;
+      dp[i] = (i == 0) ? rhs / den : (rhs - dp[i - 1]) / den;
+    }
+    M[m] = dp[m - 1];
+    for (int i = m - 2; i >= 0; --i) M[i + 1] = dp[i] - cp[i] * M[i + 2];
+  }
+  out->assign(4 * (size_t)n, 0.0);  // n-1 segments (+1 padding segment)
+  const double h2 = h * h;
+  for (int j = 0; j + 1 < n; ++j) {
+    (*out)[4 * j + 0] = y[j];
+    (*out)[4 * j + 1] = (y[j + 1] - y[j]) - h2 * (2.0 * M[j] + M[j + 1]) / 6.0;
+    (*out)[4 * j + 2] = h2 * M[j] / 2.0;
+    (*out)[4 * j + 3] = h2 * (M[j + 1] - M[j]) / 6.0;
+  }
+}
+
+double simplex_volume(int d, double edge) {
+  double v = 1.0;
+  for (int i = 1; i <= d; ++i) v *= edge / (double)i;
+  return d > 0 ? v : 1.0;
+}
+
+}  // namespace
+
+struct qiw_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  double last_ms = 0.0;
+
+  bool has_problem = false, has_P = false;
+  bool real_phase_problem = true, real_phase_P = true;
+  HostProblem hp;
+  int n_tau = 0;
+  double beta = 0.0, h = 0.0;
+  std::vector<int> dims, eoff, ptab_off, res_off, delta_kind, delta_off;
+  int64_t ptab_size = 0;
+  int res_total = 0;
+
+  DevBuf<int> d_dims, d_ptab_off, d_eoff, d_res_off, d_delta_kind, d_delta_off;
+  DevBuf<double> d_E, d_P, d_opv, d_delta;
+  DevBuf<float> d_Pf, d_opvf, d_deltaf;
+
+  std::vector<GroupRec *> groups;
+  DevBuf<DevGroup> d_groups;
+  bool groups_dirty = true;
+
+  DevBuf<DevWork> d_works;
+  DevBuf<int2> d_cta_map;
+  DevBuf<double> d_partials, d_out;
+  DevBuf<int> d_cta_first, d_res_sizes, d_out_off, d_err;
+  DevBuf<uint32_t> d_sobol;
+  int threads = 64;
+
+  int fail(int code, const std::string &msg) {
+    err = msg;
+    return code;
+  }
+  int cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return QIW_OK;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return QIW_ERR_CUDA;
+  }
+  void clear_groups() {
+    for (auto *g : groups) {
+      g->pm.release();
+      g->wj.release();
+      g->ins.release();
+      delete g;
+    }
+    groups.clear();
+    groups_dirty = true;
+  }
+  DevProblem dev_problem(bool fp32) const {
+    DevProblem p;
+    std::memset(&p, 0, sizeof(p));
+    p.S = hp.S;
+    p.n_tau = n_tau;
+    p.n_pairs = hp.n_pairs;
+    p.h = h;
+    p.inv_h = 1.0 / h;
+    p.beta = beta;
+    p.dims = d_dims.p;
+    p.ptab_off = d_ptab_off.p;
+    p.eoff = d_eoff.p;
+    p.res_off = d_res_off.p;
+    p.E = d_E.p;
+    p.P = fp32 ? (const void *)d_Pf.p : (const void *)d_P.p;
+    p.opv = fp32 ? (const void *)d_opvf.p : (const void *)d_opv.p;
+    p.delta = fp32 ? (const void *)d_deltaf.p : (const void *)d_delta.p;
+    p.delta_kind = d_delta_kind.p;
+    p.delta_off = d_delta_off.p;
+    return p;
+  }
+};
+
+extern "C" {
+
+int qiw_ctx_create(qiw_ctx **out, int device) {
+  if (!out) return QIW_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return QIW_ERR_CUDA;
+  qiw_ctx *c = new qiw_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    delete c;
+    return QIW_ERR_CUDA;
+  }
+  if (const char *t = std::getenv("QIW_THREADS")) {
+    int v = std::atoi(t);
+    if (v == 32 || v == 64 || v == 96 || v == 128) c->threads = v;
+  }
+  *out = c;
+  return QIW_OK;
+}
+
+void qiw_ctx_destroy(qiw_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  c->clear_groups();
+  c->d_groups.release();
+  for (auto *b : {&c->d_dims, &c->d_ptab_off, &c->d_eoff, &c->d_res_off, &c->d_delta_kind, &c->d_delta_off,
+                  &c->d_cta_first, &c->d_res_sizes, &c->d_out_off, &c->d_err})
+    b->release();
+  for (auto *b : {&c->d_E, &c->d_P, &c->d_opv, &c->d_delta, &c->d_partials, &c->d_out}) b->release();
+  for (auto *b : {&c->d_Pf, &c->d_opvf, &c->d_deltaf}) b->release();
+  c->d_works.release();
+  c->d_cta_map.release();
+  c->d_sobol.release();
+  cudaEventDestroy(c->ev0);
+  cudaEventDestroy(c->ev1);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char *qiw_last_error(const qiw_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+double qiw_last_kernel_ms(const qiw_ctx *c) { return c ? c->last_ms : 0.0; }
+
+int qiw_problem_set(qiw_ctx *c, const qiw_problem_desc *d) {
+  if (!c || !d) return QIW_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (d->n_sectors <= 0 || !d->sector_dims || d->n_tau < 2 || !(d->beta > 0.0) || d->n_ops <= 0 ||
+      !d->op_n_blocks || !d->op_blocks || !d->op_value_offset || !d->op_values || d->n_pairs < 0 ||
+      (d->n_pairs > 0 && (!d->pair_ops || !d->pair_prop_kind || !d->pair_prop_data)) || !d->atomic_energies)
+    return c->fail(QIW_ERR_ARG, "qiw_problem_set: missing or invalid field");
+  c->clear_groups();
+  HostProblem &hp = c->hp;
+  std::string e;
+  int prc = host_problem_from_desc(d, &hp, &e);
+  if (prc) return c->fail(prc, "qiw_problem_set: " + e);
+  const int64_t max_val = (int64_t)hp.op_vals.size();
+  c->real_phase_problem = true;
+  std::vector<double> opv(max_val), E;
+  std::vector<float> opvf(max_val);
+  for (int64_t i = 0; i < max_val; ++i) {
+    if (hp.op_vals[i].imag() != 0.0) c->real_phase_problem = false;
+    opv[i] = hp.op_vals[i].real();
+    opvf[i] = (float)opv[i];
+  }
+  c->n_tau = d->n_tau;
+  c->beta = d->beta;
+  c->h = d->beta / (double)(d->n_tau - 1);
+  c->delta_kind.resize(hp.n_pairs);
+  c->delta_off.resize(hp.n_pairs);
+  std::vector<double> delta;
+  for (int p = 0; p < hp.n_pairs; ++p) {
+    int kind = d->pair_prop_kind[p];
+    if (kind != QIW_PROP_LINEAR && kind != QIW_PROP_CUBIC) return c->fail(QIW_ERR_ARG, "qiw_problem_set: unknown propagator kind");
+    std::vector<double> y(c->n_tau);
+    for (int j = 0; j < c->n_tau; ++j) {
+      const double re = d->pair_prop_data[2 * ((size_t)p * c->n_tau + j)];
+      const double im = d->pair_prop_data[2 * ((size_t)p * c->n_tau + j) + 1];
+      if (re != 0.0) c->real_phase_problem = false;
+      y[j] = -im;  // i * Delta
+    }
+    c->delta_kind[p] = kind;
+    c->delta_off[p] = (int)delta.size();
+    if (kind == QIW_PROP_LINEAR) delta.insert(delta.end(), y.begin(), y.end());
+    else {
+      std::vector<double> co;
+      cubic_coeffs(y, c->h, &co);
+      delta.insert(delta.end(), co.begin(), co.end());
+    }
+  }
+  c->dims = hp.dims;
+  c->eoff.resize(hp.S);
+  c->ptab_off.resize(hp.S);
+  c->res_off.resize(hp.S);
+  int eo = 0, ro = 0;
+  int64_t po = 0;
+  for (int s = 0; s < hp.S; ++s) {
+    c->eoff[s] = eo;
+    eo += hp.dims[s];
+    c->res_off[s] = ro;
+    ro += hp.dims[s] * hp.dims[s];
+    c->ptab_off[s] = (int)po;
+    po += (int64_t)c->n_tau * hp.dims[s] * hp.dims[s];
+  }
+  c->ptab_size = po;
+  c->res_total = ro;
+  E.assign(d->atomic_energies, d->atomic_energies + eo);
+  std::vector<float> deltaf(delta.begin(), delta.end());
+  cudaStream_t st = c->stream;
+  int rc;
+  if ((rc = c->cuda(c->d_dims.upload(hp.dims.data(), hp.S, st), "upload dims")) ||
+      (rc = c->cuda(c->d_ptab_off.upload(c->ptab_off.data(), hp.S, st), "upload ptab_off")) ||
+      (rc = c->cuda(c->d_eoff.upload(c->eoff.data(), hp.S, st), "upload eoff")) ||
+      (rc = c->cuda(c->d_res_off.upload(c->res_off.data(), hp.S, st), "upload res_off")) ||
+      (rc = c->cuda(c->d_E.upload(E.data(), E.size(), st), "upload energies")) ||
+      (rc = c->cuda(c->d_opv.upload(opv.data(), opv.size(), st), "upload operators")) ||
+      (rc = c->cuda(c->d_opvf.upload(opvf.data(), opvf.size(), st), "upload operators")) ||
+      (rc = c->cuda(c->d_delta.upload(delta.data(), delta.size(), st), "upload delta")) ||
+      (rc = c->cuda(c->d_deltaf.upload(deltaf.data(), deltaf.size(), st), "upload delta")) ||
+      (rc = c->cuda(c->d_delta_kind.upload(c->delta_kind.data(), c->delta_kind.size(), st), "upload delta kind")) ||
+      (rc = c->cuda(c->d_delta_off.upload(c->delta_off.data(), c->delta_off.size(), st), "upload delta off")) ||
+      (rc = c->cuda(c->d_P.reserve(po), "alloc P")) || (rc = c->cuda(c->d_Pf.reserve(po), "alloc P")) ||
+      (rc = c->cuda(cudaStreamSynchronize(st), "problem upload")))
+    return rc;
+  c->has_problem = true;
+  c->has_P = false;
+  return QIW_OK;
+}
+
+int qiw_ppgf_set(qiw_ctx *c, const double *P) {
+  if (!c || !P) return QIW_ERR_ARG;
+  if (!c->has_problem) return c->fail(QIW_ERR_ARG, "qiw_ppgf_set: no problem set");
+  cudaSetDevice(c->device);
+  std::vector<double> t(c->ptab_size);
+  std::vector<float> tf(c->ptab_size);
+  c->real_phase_P = true;
+  for (int64_t i = 0; i < c->ptab_size; ++i) {
+    if (P[2 * i] != 0.0) c->real_phase_P = false;
+    t[i] = -P[2 * i + 1];  // i * P
+    tf[i] = (float)t[i];
+  }
+  int rc;
+  if ((rc = c->cuda(c->d_P.upload(t.data(), t.size(), c->stream), "upload P")) ||
+      (rc = c->cuda(c->d_Pf.upload(tf.data(), tf.size(), c->stream), "upload P")) ||
+      (rc = c->cuda(cudaStreamSynchronize(c->stream), "upload P")))
+    return rc;
+  c->has_P = true;
+  return QIW_OK;
+}
+
+int qiw_group_create(qiw_ctx *c, const qiw_group_desc *d, int32_t *group_id) {
+  if (!c || !d || !group_id) return QIW_ERR_ARG;
+  if (!c->has_problem) return c->fail(QIW_ERR_ARG, "qiw_group_create: no problem set");
+  cudaSetDevice(c->device);
+  GroupSpec gs;
+  {
+    std::string e;
+    int grc = group_spec_from_desc(d, &gs, &e);
+    if (grc) return c->fail(grc, "qiw_group_create: " + e);
+  }
+  PlanOptions opt;
+  opt.arena_budget = kArenaLarge;
+  if (const char *b = std::getenv("QIW_ARENA_BUDGET")) opt.arena_budget = std::max<int64_t>(256, std::atoll(b));
+  opt.arena_budget = std::min<int64_t>(opt.arena_budget, kArenaLarge);
+  GroupRec *g = new GroupRec();
+  std::string e;
+  int rc = plan_group(c->hp, gs, opt, &g->plan, &e);
+  if (rc) {
+    delete g;
+    return c->fail(rc, "qiw_group_create: " + e);
+  }
+  if (arena_class(g->plan.arena) < 0) {
+    delete g;
+    return c->fail(QIW_ERR_MEMORY, "qiw_group_create: per-sample arena above the largest kernel instantiation");
+  }
+  const Plan &p = g->plan;
+  if ((rc = c->cuda(g->pm.upload(p.pm.data(), p.pm.size(), c->stream), "upload plan")) ||
+      (rc = c->cuda(g->wj.upload(p.wj.data(), p.wj.size(), c->stream), "upload plan")) ||
+      (rc = c->cuda(g->ins.upload(p.ins.data(), p.ins.size(), c->stream), "upload plan")) ||
+      (rc = c->cuda(cudaStreamSynchronize(c->stream), "upload plan"))) {
+    delete g;
+    return rc;
+  }
+  DevGroup &dg = g->dg;
+  std::memset(&dg, 0, sizeof(dg));
+  dg.kind = p.kind;
+  dg.order = p.order;
+  dg.n_nodes = p.n_nodes;
+  dg.D = p.D;
+  dg.d_before = p.d_before;
+  dg.d_after = p.d_after;
+  dg.use_bold = p.use_bold;
+  dg.n_fixed = p.n_fixed;
+  for (int f = 0; f < p.n_fixed; ++f) {
+    dg.fixed_pos[f] = p.fixed_pos[f];
+    dg.fixed_time[f] = p.fixed_time[f];
+  }
+  for (size_t j = 0; j < p.var_pos.size(); ++j) dg.var_pos[j] = p.var_pos[j];
+  dg.n_pm = (int)p.pm.size();
+  dg.n_w = (int)p.wj.size();
+  dg.n_instr = (int)p.ins.size();
+  dg.arena = (int)p.arena;
+  dg.res_size = p.res_size;
+  dg.pm = g->pm.p;
+  dg.wj = g->wj.p;
+  dg.ins = g->ins.p;
+  c->groups.push_back(g);
+  c->groups_dirty = true;
+  *group_id = (int32_t)c->groups.size() - 1;
+  return QIW_OK;
+}
+
+int qiw_group_stats_get(qiw_ctx *c, int32_t gid, qiw_group_stats *out) {
+  if (!c || !out || gid < 0 || gid >= (int)c->groups.size()) return QIW_ERR_ARG;
+  const Plan &p = c->groups[gid]->plan;
+  out->n_nodes_dag = p.dag_nodes;
+  out->n_instructions = (int64_t)p.ins.size();
+  out->arena_elements = p.arena;
+  out->flops_per_sample = p.flops;
+  out->tree_flops_per_sample = p.tree_flops;
+  out->n_leaves_tree = p.tree_leaves;
+  return QIW_OK;
+}
+
+int qiw_integrate(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, double *out) {
+  if (!c || n_work < 0 || (n_work > 0 && (!work || !out))) return QIW_ERR_ARG;
+  if (precision != QIW_PREC_FP64 && precision != QIW_PREC_FP32) return c->fail(QIW_ERR_ARG, "qiw_integrate: unknown precision");
+  if (!c->has_problem) return c->fail(QIW_ERR_ARG, "qiw_integrate: no problem set");
+  cudaSetDevice(c->device);
+  if (n_work == 0) return QIW_OK;
+  bool need_P = false;
+  std::vector<DevWork> works(n_work);
+  std::vector<int2> cta_map;
+  std::vector<int> cta_first(n_work), res_sizes(n_work), out_off(n_work);
+  std::vector<uint32_t> sob;
+  int64_t arena_max = 0;
+  int res_max = 0, out_total = 0;
+  const int threads = c->threads;
+  for (int i = 0; i < n_work; ++i) {
+    const qiw_work_desc &wd = work[i];
+    if (wd.group < 0 || wd.group >= (int)c->groups.size()) return c->fail(QIW_ERR_ARG, "qiw_integrate: bad group id");
+    const Plan &p = c->groups[wd.group]->plan;
+    if (p.use_bold) need_P = true;
+    if (p.D > 0 && (!wd.sobol_m || !wd.sobol_x0)) return c->fail(QIW_ERR_ARG, "qiw_integrate: Sobol tables missing");
+    if (!(wd.t_i <= wd.t_f) || (p.kind != QIW_GROUP_BARE && !(wd.t_i <= wd.t_w && wd.t_w <= wd.t_f)))
+      return c->fail(QIW_ERR_ARG, "qiw_integrate: times must satisfy t_i <= t_w <= t_f");
+    if (p.D > 0 && (wd.n_total == 0 || wd.first_index + wd.n_samples > (1ull << 32)))
+      return c->fail(QIW_ERR_ARG, "qiw_integrate: Sobol index range beyond 2^32 or N_total = 0");
+    DevWork &w = works[i];
+    std::memset(&w, 0, sizeof(w));
+    w.group = wd.group;
+    w.t_i = wd.t_i;
+    w.t_w = wd.t_w;
+    w.t_f = wd.t_f;
+    w.first_index = wd.first_index;
+    if (p.D == 0) {
+      w.n_samples = 1;
+      w.scale = 1.0;  // order 0: evaluated exactly, no qMC average
+    } else {
+      w.n_samples = wd.n_samples;
+      double J = (p.kind == QIW_GROUP_BARE)
+                     ? simplex_volume(p.D, wd.t_f - wd.t_i)
+                     : simplex_volume(p.d_before, wd.t_w - wd.t_i) * simplex_volume(p.d_after, wd.t_f - wd.t_w);
+      w.scale = J / (double)wd.n_total;
+    }
+    w.n_cta = (int)((w.n_samples + threads - 1) / threads);
+    cta_first[i] = (int)cta_map.size();
+    for (int k = 0; k < w.n_cta; ++k) cta_map.push_back(make_int2(i, k * threads));
+    res_sizes[i] = p.res_size;
+    out_off[i] = out_total;
+    out_total += p.res_size;
+    arena_max = std::max<int64_t>(arena_max, p.arena);
+    res_max = std::max(res_max, p.res_size);
+    // Sobol tables: stash host offsets in the pointer fields, patched after upload
+    w.m = reinterpret_cast<const uint32_t *>((uintptr_t)sob.size());
+    if (p.D > 0) sob.insert(sob.end(), wd.sobol_m, wd.sobol_m + 32 * p.D);
+    w.x0 = reinterpret_cast<const uint32_t *>((uintptr_t)sob.size());
+    if (p.D > 0) sob.insert(sob.end(), wd.sobol_x0, wd.sobol_x0 + p.D);
+  }
+  if (!c->real_phase_problem || (need_P && !c->real_phase_P))
+    return c->fail(QIW_ERR_UNSUPPORTED, "qiw_integrate: inputs are not real-phase (i*P, i*Delta and operator "
+                                        "blocks must be real); only the real-phase kernels are built");
+  if (need_P && !c->has_P) return c->fail(QIW_ERR_ARG, "qiw_integrate: bold group but qiw_ppgf_set was not called");
+  if (res_max > kResLarge) return c->fail(QIW_ERR_UNSUPPORTED, "qiw_integrate: sum of d_s^2 above 512");
+  int rc;
+  cudaStream_t st = c->stream;
+  if ((rc = c->cuda(c->d_sobol.upload(sob.data(), sob.size(), st), "upload Sobol"))) return rc;
+  for (auto &w : works) {
+    w.m = c->d_sobol.p + (uintptr_t)w.m;
+    w.x0 = c->d_sobol.p + (uintptr_t)w.x0;
+  }
+  if (c->groups_dirty) {
+    std::vector<DevGroup> dgs;
+    for (auto *g : c->groups) dgs.push_back(g->dg);
+    if ((rc = c->cuda(c->d_groups.upload(dgs.data(), dgs.size(), st), "upload groups"))) return rc;
+    c->groups_dirty = false;
+  }
+  const int n_cta = (int)cta_map.size();
+  int zero = 0;
+  if ((rc = c->cuda(c->d_works.upload(works.data(), works.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_cta_map.upload(cta_map.data(), cta_map.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_cta_first.upload(cta_first.data(), cta_first.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_res_sizes.upload(res_sizes.data(), res_sizes.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_out_off.upload(out_off.data(), out_off.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_err.upload(&zero, 1, st), "upload work")) ||
+      (rc = c->cuda(c->d_partials.reserve((size_t)n_cta * res_max), "alloc partials")) ||
+      (rc = c->cuda(c->d_out.reserve((size_t)2 * out_total), "alloc out")))
+    return rc;
+  LaunchArgs la;
+  la.pb = c->dev_problem(precision == QIW_PREC_FP32);
+  la.groups = c->d_groups.p;
+  la.works = c->d_works.p;
+  la.cta_map = c->d_cta_map.p;
+  la.partials = c->d_partials.p;
+  la.n_cta = n_cta;
+  la.threads = threads;
+  la.arena_max = arena_max;
+  la.res_max = res_max;
+  la.fp32 = precision == QIW_PREC_FP32;
+  la.stream = st;
+  FinishArgs fa;
+  fa.works = c->d_works.p;
+  fa.cta_first = c->d_cta_first.p;
+  fa.partials = c->d_partials.p;
+  fa.res_sizes = c->d_res_sizes.p;
+  fa.out_off = c->d_out_off.p;
+  fa.out = c->d_out.p;
+  fa.err_word = c->d_err.p;
+  fa.n_work = n_work;
+  fa.stream = st;
+  if ((rc = c->cuda(cudaEventRecord(c->ev0, st), "event")) ||
+      (n_cta > 0 && (rc = c->cuda(launch_eval(la), "eval kernel launch"))) ||
+      (rc = c->cuda(launch_finish(fa), "finish kernel launch")) || (rc = c->cuda(cudaEventRecord(c->ev1, st), "event")))
+    return rc;
+  int err_word = 0;
+  if ((rc = c->cuda(cudaMemcpyAsync(out, c->d_out.p, sizeof(double) * 2 * out_total, cudaMemcpyDeviceToHost, st), "copy out")) ||
+      (rc = c->cuda(cudaMemcpyAsync(&err_word, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "copy err")) ||
+      (rc = c->cuda(cudaStreamSynchronize(st), "integrate")))
+    return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->last_ms = ms;
+  if (err_word) return c->fail(QIW_ERR_DEVICE, "qiw_integrate: non-finite result detected on the device");
+  return QIW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,335 @@
+// CUDA kernels of the qMC diagram integration (sm_103a).
+//
+// One thread evaluates one qMC sample of one topology group:
+//   1. Sobol point by Gray-code jump   x = x0 ^ XOR_{b in bits(n ^ n>>1)} m[:, b]
+//      (src/scrambled_sobol.jl:158-173, bit-exact UInt32 arithmetic);
+//   2. Root / DoubleSimplexRoot map onto ordered times (src/qmc_integrate.jl:229-238, 425-449);
+//   3. i*P(t_{j+1}-t_j) blocks by linear interpolation of the P table, or the exact atomic
+//      i*P0 = exp(-dt E) for the bare step (src/topology_eval.jl:357-374,
+//      src/exact_atomic_ppgf.jl:109-118); i*Delta_p weights (src/topology_eval.jl:412-415);
+//   4. the group's program: the merged configuration DAG built by the host planner.
+// All threads of a CTA run the same (warp-uniform) instruction stream, so control flow never
+// diverges; per-sample matrices live in the thread's arena (local memory, L1 resident).
+//
+// Real-phase arithmetic: on the imaginary branch i*P, i*Delta and the operator blocks are
+// real, so every complex product of the reference has exactly zero cross terms; the host
+// verifies that and the kernels compute the real parts only (the result is -i times it).
+//
+// Reduction: per-thread sector-block sums -> warp shuffles -> CTA shared memory (fixed
+// order) -> per-CTA partials -> one CTA per work item sums its partials in order with
+// Kahan compensation.  Re-runs are bit-identical.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "qiw_internal.hpp"
+#include "qiw_kernels.hpp"
+
+namespace qiw {
+
+template <typename T>
+__device__ __forceinline__ T fmaT(T a, T b, T c);
+template <>
+__device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return fma(a, b, c); }
+template <>
+__device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+__device__ __forceinline__ Instr load_instr(const Instr *p) {
+  const int4 *q = reinterpret_cast<const int4 *>(p);
+  int4 a = __ldg(q), b = __ldg(q + 1);
+  Instr I;
+  int4 *o = reinterpret_cast<int4 *>(&I);
+  o[0] = a;
+  o[1] = b;
+  return I;
+}
+
+// Linear interpolation of a uniform-grid table at dt >= 0 (rule of qiw/gf.py: linear_interp).
+__device__ __forceinline__ void lin_index(double dt, double inv_h, int n_tau, int *i, double *f) {
+  double x = dt * inv_h;
+  int k = (int)floor(x);
+  k = k > n_tau - 2 ? n_tau - 2 : k;
+  k = k < 0 ? 0 : k;
+  *i = k;
+  *f = x - (double)k;
+}
+
+template <typename T, int ARENA, int RESMAX>
+__global__ void __launch_bounds__(kMaxThreads)
+    eval_kernel(DevProblem pb, const DevGroup *__restrict__ groups, const DevWork *__restrict__ works,
+                const int2 *__restrict__ cta_map, double *__restrict__ partials) {
+  const int2 cm = cta_map[blockIdx.x];
+  const DevWork &w = works[cm.x];
+  const DevGroup &g = groups[w.group];
+  const uint64_t sidx = (uint64_t)cm.y + threadIdx.x;
+  const bool active = sidx < w.n_samples;
+  const int res_size = g.res_size;
+
+  T A[ARENA];
+  double R[RESMAX];
+#pragma unroll 1
+  for (int e = 0; e < res_size; ++e) R[e] = 0.0;
+
+  if (active) {
+    double tm[kMaxNodes];
+    const double tsel[3] = {w.t_i, w.t_w, w.t_f};
+#pragma unroll 1
+    for (int f = 0; f < g.n_fixed; ++f) tm[g.fixed_pos[f]] = tsel[g.fixed_time[f]];
+    const int D = g.D;
+    if (D > 0) {
+      const uint64_t n = w.first_index + sidx;
+      const uint32_t gray = (uint32_t)(n ^ (n >> 1));
+      double u[kMaxDim];
+#pragma unroll 1
+      for (int d = 0; d < D; ++d) {
+        uint32_t v = __ldg(w.x0 + d);
+        const uint32_t *md = w.m + d * 32;
+#pragma unroll 8
+        for (int b = 0; b < 32; ++b)
+          if ((gray >> b) & 1u) v ^= __ldg(md + b);
+        u[d] = ldexp((double)v, -32);  // exact: ldexp(Float64(x), -32)
+      }
+      if (g.kind == 1) {  // RootTransform over [t_i, t_f]
+        const double u_diff = w.t_f - w.t_i;
+        double acc = pow(u[0], 1.0 / (double)D);
+        u[0] = acc;
+#pragma unroll 1
+        for (int i = 2; i <= D; ++i) {
+          acc = acc * pow(u[i - 1], 1.0 / (double)(D - i + 1));
+          u[i - 1] = acc;
+        }
+#pragma unroll 1
+        for (int i = 0; i < D; ++i) u[i] = w.t_i + u[i] * u_diff;
+      } else {  // DoubleSimplexRootTransform
+        const int dg = g.d_after, dl = g.d_before;
+        const double fw = w.t_f - w.t_w, wi = w.t_w - w.t_i;
+        double acc = pow(u[0], 1.0 / (double)dg);
+        u[0] = acc;
+#pragma unroll 1
+        for (int i = 2; i <= dg; ++i) {
+          acc = acc * pow(u[i - 1], 1.0 / (double)(dg - i + 1));
+          u[i - 1] = acc;
+        }
+#pragma unroll 1
+        for (int i = 0; i < dg; ++i) u[i] = u[i] * fw + w.t_w;
+        if (dl > 0) {
+          acc = pow(u[dg], 1.0 / (double)dl);
+          u[dg] = acc;
+#pragma unroll 1
+          for (int i = dg + 2; i <= D; ++i) {
+            acc = acc * pow(u[i - 1], 1.0 / (double)(D - i + 1));
+            u[i - 1] = acc;
+          }
+#pragma unroll 1
+          for (int i = dg; i < D; ++i) u[i] = u[i] * wi + w.t_i;
+        }
+      }
+#pragma unroll 1
+      for (int j = 0; j < D; ++j) tm[g.var_pos[j]] = u[j];
+    }
+
+    // i*P blocks of the intervals the program uses.
+    const T *Ptab = reinterpret_cast<const T *>(pb.P);
+#pragma unroll 1
+    for (int j = 0; j < g.n_pm; ++j) {
+      const PmJob job = g.pm[j];
+      double dt = tm[job.iv + 1] - tm[job.iv];
+      dt = dt < 0.0 ? 0.0 : dt;  // time-ordering violations from rounding (topology_eval.jl:361-364)
+      const int d = pb.dims[job.s];
+      if (g.use_bold) {
+        int i;
+        double f;
+        lin_index(dt, pb.inv_h, pb.n_tau, &i, &f);
+        const T *a = Ptab + pb.ptab_off[job.s] + (size_t)i * d * d;
+        const T ff = (T)f;
+#pragma unroll 1
+        for (int e = 0; e < d * d; ++e) {
+          const T lo = __ldg(a + e), hi = __ldg(a + d * d + e);
+          A[job.off + e] = fmaT<T>(ff, hi - lo, lo);
+        }
+      } else {
+        const double *E = pb.E + pb.eoff[job.s];
+#pragma unroll 1
+        for (int e = 0; e < d; ++e) A[job.off + e] = (T)exp(-dt * __ldg(E + e));
+      }
+    }
+    // i*Delta weights.
+    const T *Dtab = reinterpret_cast<const T *>(pb.delta);
+#pragma unroll 1
+    for (int j = 0; j < g.n_w; ++j) {
+      const WJob job = g.wj[j];
+      double dt = tm[job.tail] - tm[job.head];
+      dt = dt < 0.0 ? 0.0 : dt;  // topology_eval.jl:407-410
+      int i;
+      double f;
+      lin_index(dt, pb.inv_h, pb.n_tau, &i, &f);
+      const T *t = Dtab + pb.delta_off[job.pair];
+      T val;
+      if (pb.delta_kind[job.pair] == 0) {
+        const T lo = __ldg(t + i), hi = __ldg(t + i + 1);
+        val = fmaT<T>((T)f, hi - lo, lo);
+      } else {  // natural cubic spline, per-segment polynomial in f
+        const T *c = t + 4 * i;
+        const T ff = (T)f;
+        val = fmaT<T>(ff, fmaT<T>(ff, fmaT<T>(ff, __ldg(c + 3), __ldg(c + 2)), __ldg(c + 1)), __ldg(c));
+      }
+      A[job.off] = val;
+    }
+
+    // The group's program.
+    const T *O = reinterpret_cast<const T *>(pb.opv);
+    const int n_ins = g.n_instr;
+#pragma unroll 1
+    for (int ip = 0; ip < n_ins; ++ip) {
+      const Instr I = load_instr(g.ins + ip);
+      const int rows = I.rows, cols = I.cols;
+      switch (I.op) {
+        case OP_LOADP: {
+          const T c = (T)I.c;
+          if (I.inner) {
+#pragma unroll 1
+            for (int j = 0; j < rows; ++j)
+#pragma unroll 1
+              for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = (r == j) ? c * A[I.a + r] : (T)0;
+          } else {
+#pragma unroll 1
+            for (int e = 0; e < rows * rows; ++e) A[I.dst + e] = c * A[I.a + e];
+          }
+          break;
+        }
+        case OP_LOADC: {
+          const T c = (T)I.c;
+#pragma unroll 1
+          for (int e = 0; e < rows * cols; ++e) A[I.dst + e] = c * __ldg(O + I.a + e);
+          break;
+        }
+        case OP_PMUL: {
+#pragma unroll 1
+          for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+            for (int r = 0; r < rows; ++r) {
+              T acc = (T)0;
+#pragma unroll 1
+              for (int k = 0; k < rows; ++k) acc = fmaT<T>(A[I.a + k * rows + r], A[I.src + j * rows + k], acc);
+              A[I.dst + j * rows + r] = acc;
+            }
+          break;
+        }
+        case OP_PMULD: {
+#pragma unroll 1
+          for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+            for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = A[I.a + r] * A[I.src + j * rows + r];
+          break;
+        }
+        case OP_OMUL: {
+          const int inner = I.inner;
+          const T coef = (I.w >= 0) ? (T)I.c * A[I.w] : (T)I.c;
+#pragma unroll 1
+          for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+            for (int r = 0; r < rows; ++r) {
+              T acc = (T)0;
+#pragma unroll 1
+              for (int k = 0; k < inner; ++k) acc = fmaT<T>(__ldg(O + I.a + k * rows + r), A[I.src + j * inner + k], acc);
+              const int o = I.dst + j * rows + r;
+              A[o] = I.acc ? fmaT<T>(coef, acc, A[o]) : coef * acc;
+            }
+          break;
+        }
+        case OP_AXPY: {
+          const T coef = (I.w >= 0) ? (T)I.c * A[I.w] : (T)I.c;
+#pragma unroll 1
+          for (int e = 0; e < rows * cols; ++e) {
+            const int o = I.dst + e;
+            A[o] = I.acc ? fmaT<T>(coef, A[I.src + e], A[o]) : coef * A[I.src + e];
+          }
+          break;
+        }
+        case OP_LEAF: {
+#pragma unroll 1
+          for (int e = 0; e < rows * cols; ++e) R[I.a + e] += (double)A[I.src + e];
+          break;
+        }
+        default:
+          break;
+      }
+    }
+  }
+
+  // Deterministic CTA reduction of R -> partials[blockIdx.x][res_size].
+  __shared__ double red[kMaxThreads / 32][RESMAX];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n_warps = (blockDim.x + 31) >> 5;
+#pragma unroll 1
+  for (int e = 0; e < res_size; ++e) {
+    double v = R[e];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][e] = v;
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int e = threadIdx.x; e < res_size; e += blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < n_warps; ++k) s += red[k][e];
+    partials[(size_t)blockIdx.x * res_size + e] = s;
+  }
+}
+
+// out[w][e] = -i * scale_w * sum_c partials[c][e] over the CTAs of work item w (in order,
+// Kahan-compensated).  Sets *err_word if a result is not finite.
+__global__ void finish_kernel(const DevWork *__restrict__ works, const int *__restrict__ cta_first,
+                              const double *__restrict__ partials, const int *__restrict__ res_sizes,
+                              const int *__restrict__ out_off, double *__restrict__ out,
+                              int *__restrict__ err_word) {
+  const int wi = blockIdx.x;
+  const DevWork &w = works[wi];
+  const int rs = res_sizes[wi];
+  const int c0 = cta_first[wi];
+  for (int e = threadIdx.x; e < rs; e += blockDim.x) {
+    double s = 0.0, comp = 0.0;
+    for (int c = 0; c < w.n_cta; ++c) {
+      double y = partials[(size_t)(c0 + c) * rs + e] - comp;
+      double t = s + y;
+      comp = (t - s) - y;
+      s = t;
+    }
+    const double v = -w.scale * s;
+    if (!isfinite(v)) atomicOr(err_word, 1);
+    out[2 * ((size_t)out_off[wi] + e)] = 0.0;
+    out[2 * ((size_t)out_off[wi] + e) + 1] = v;
+  }
+}
+
+template <typename T, int ARENA, int RESMAX>
+static cudaError_t launch_t(const LaunchArgs &a) {
+  eval_kernel<T, ARENA, RESMAX><<<a.n_cta, a.threads, 0, a.stream>>>(a.pb, a.groups, a.works, a.cta_map,
+                                                                       a.partials);
+  return cudaGetLastError();
+}
+
+int arena_class(int64_t arena) {
+  if (arena <= kArenaSmall) return 0;
+  if (arena <= kArenaLarge) return 1;
+  return -1;
+}
+
+cudaError_t launch_eval(const LaunchArgs &a) {
+  const bool big_res = a.res_max > kResSmall;
+  const int ac = arena_class(a.arena_max);
+  if (a.fp32) {
+    if (ac == 0) return big_res ? launch_t<float, kArenaSmall, kResLarge>(a) : launch_t<float, kArenaSmall, kResSmall>(a);
+    return big_res ? launch_t<float, kArenaLarge, kResLarge>(a) : launch_t<float, kArenaLarge, kResSmall>(a);
+  }
+  if (ac == 0) return big_res ? launch_t<double, kArenaSmall, kResLarge>(a) : launch_t<double, kArenaSmall, kResSmall>(a);
+  return big_res ? launch_t<double, kArenaLarge, kResLarge>(a) : launch_t<double, kArenaLarge, kResSmall>(a);
+}
+
+cudaError_t launch_finish(const FinishArgs &a) {
+  finish_kernel<<<a.n_work, 128, 0, a.stream>>>(a.works, a.cta_first, a.partials, a.res_sizes, a.out_off,
+                                               a.out, a.err_word);
+  return cudaGetLastError();
+}
+
+}  // namespace qiw

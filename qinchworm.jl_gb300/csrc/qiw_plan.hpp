@@ -1,0 +1,68 @@
+// Host-side planner: turns one topology group into a sample-independent program.
+#pragma once
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "qiw_internal.hpp"
+
+namespace qiw {
+
+using cd = std::complex<double>;
+
+struct HostProblem {
+  int S = 0;
+  std::vector<int> dims;
+  int n_ops = 0;
+  std::vector<int> op_target;          // [n_ops * S], -1: no block
+  std::vector<int64_t> op_valoff;      // [n_ops * S] complex-element offset, column-major d_f x d_i
+  std::vector<cd> op_vals;
+  int identity_op = 0;
+  int n_pairs = 0;
+  std::vector<int> pair_op_i, pair_op_f;
+  int target(int op, int s) const { return op_target[(size_t)op * S + s]; }
+};
+
+struct GroupSpec {
+  int kind = 0, order = 0, n_pts_after = 0;
+  int corr_A = -1, corr_B = -1;
+  std::vector<std::vector<std::pair<int, int>>> tops;   // 1-based vertex pairs
+  std::vector<int> parity;
+};
+
+struct PlanOptions {
+  int64_t arena_budget = 4096;   // per-sample working-set budget (elements)
+  bool fold_scalar_ops = true;   // fold 1x1 operator blocks into coefficients
+};
+
+struct Plan {
+  int kind = 0, order = 0, n_nodes = 0, D = 0, d_before = 0, d_after = 0;
+  int use_bold = 1;
+  int n_fixed = 0;
+  int fixed_pos[kMaxFixed] = {0, 0, 0};
+  int fixed_time[kMaxFixed] = {0, 0, 0};
+  std::vector<int> var_pos;
+  std::vector<Instr> ins;
+  std::vector<PmJob> pm;
+  std::vector<WJob> wj;
+  int64_t arena = 0;
+  int res_size = 0;
+  int64_t dag_nodes = 0;
+  double flops = 0.0;            // per sample, real-phase count (x4 for complex)
+  double tree_flops = 0.0;       // per sample, reference tree (complex arithmetic)
+  int64_t tree_leaves = 0;
+  int n_batches = 0;
+};
+
+// Returns 0 on success, a QIW_ERR_* code otherwise (message in *err).
+int plan_group(const HostProblem &pb, const GroupSpec &g, const PlanOptions &opt, Plan *out,
+               std::string *err);
+
+}  // namespace qiw
+
+namespace qiw {
+// Conversions from the C-ABI descriptors (no CUDA involved).
+int host_problem_from_desc(const void *problem_desc, HostProblem *hp, std::string *err);
+int group_spec_from_desc(const void *group_desc, GroupSpec *gs, std::string *err);
+
+}  // namespace qiw

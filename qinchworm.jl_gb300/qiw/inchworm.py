@@ -1,0 +1,346 @@
+"""Host mirror of the reference's inchworm driver (`src/inchworm.jl`) on the GPU path.
+
+Same entry points, argument meaning and results as the reference:
+  * `inchworm_step`, `inchworm_step_bare`  (src/inchworm.jl:123-304)
+  * `inchworm`  == inchworm!               (src/inchworm.jl:332-498)
+  * `correlator_2p`                        (src/inchworm.jl:805-1084)
+Every qMC integral -- the `contour_integral(t -> eval(td.topologies, t), ...)` closures -- runs
+in the CUDA library; one inch step issues a single launch covering all its topology groups.
+The host keeps what the reference keeps on the host: topology generation, set_ppgf!,
+normalize! and the (optional) rank decomposition and all-reduce.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from . import ppgf as _ppgf
+from .device import Device, Work, blocks_to_sbm
+from .diagrammatics import Topology, get_topologies_at_order
+from .ed import SectorBlockMatrix
+from .gf import ImaginaryTimeGF
+from .sobol import direction_numbers, scramble
+
+
+@dataclass
+class RandomizationParams:
+    """src/randomization.jl:46-57: rng None means unscrambled (and one sequence)."""
+    rng: Optional[object] = None
+    N_seqs: int = 1
+    target_std: float = 0.0
+
+
+@dataclass
+class TopologiesInputData:
+    """src/inchworm.jl:76-87."""
+    order: int
+    n_pts_after: int
+    topologies: List[Topology]
+    N_samples: int
+    rand_params: RandomizationParams = field(default_factory=RandomizationParams)
+
+
+class Comm:
+    """Rank decomposition of the sample range (src/mpi.jl:49-54, 104-127).  The default is a
+    single rank; `TorchComm` provides an all-reduce over torch.distributed."""
+    rank = 0
+    size = 1
+
+    def allreduce(self, v: np.ndarray) -> np.ndarray:
+        return v
+
+
+class TorchComm(Comm):
+    def __init__(self):
+        import torch.distributed as dist
+        self.dist = dist
+        self.rank = dist.get_rank()
+        self.size = dist.get_world_size()
+
+    def allreduce(self, v: np.ndarray) -> np.ndarray:
+        import torch
+        t = torch.from_numpy(np.ascontiguousarray(v))
+        self.dist.all_reduce(t)
+        return t.numpy()
+
+
+def split_count(N: int, n: int) -> List[int]:
+    q, r = divmod(N, n)
+    return [q + 1 if i < r else q for i in range(n)]
+
+
+def rank_sub_range(N: int, comm: Comm) -> Tuple[int, int]:
+    """0-based (start, length) of this rank's chunk."""
+    chunks = split_count(N, comm.size)
+    return sum(chunks[:comm.rank]), chunks[comm.rank]
+
+
+def _pack_blocks(blocks: List[np.ndarray]) -> np.ndarray:
+    return np.concatenate([b.ravel(order="F") for b in blocks])
+
+
+def _unpack_blocks(v: np.ndarray, dims) -> List[np.ndarray]:
+    out, o = [], 0
+    for d in dims:
+        out.append(v[o:o + d * d].reshape(d, d, order="F").copy())
+        o += d * d
+    return out
+
+
+class _Session:
+    """Per-run state: device, problem upload and planned groups."""
+
+    def __init__(self, dev: Optional[Device], expansion):
+        self.dev = dev if dev is not None else Device(0)
+        if getattr(self.dev, "_expansion", None) is not expansion:
+            self.dev.set_problem(expansion)
+            self.dev._expansion = expansion
+            self.dev._groups = {}
+        self.exp = expansion
+
+    def group(self, kind: int, td: TopologiesInputData, corr: Optional[int] = None) -> int:
+        key = (kind, td.order, td.n_pts_after, corr, tuple((t.pairs, t.parity) for t in td.topologies))
+        g = self.dev._groups.get(key)
+        if g is None:
+            g = self.dev.create_group(kind, td.order, td.n_pts_after, td.topologies, corr)
+            self.dev._groups[key] = g
+        return g
+
+    def run(self, kind: int, tds: Sequence[TopologiesInputData], t_i, t_w, t_f, precision, comm: Comm,
+            corr: Optional[int] = None):
+        """All groups of a step; returns per group (mean blocks, std blocks or None)."""
+        dims = self.exp.dims
+        plan = []
+        for td in tds:
+            if td.order > 0 and td.N_samples <= 0:
+                plan.append(None)
+                continue
+            gid = self.group(kind, td, corr)
+            D = 2 * td.order
+            seqs = []
+            n_seqs = 1 if td.order == 0 else td.rand_params.N_seqs
+            for s in range(n_seqs):
+                if D == 0 or td.rand_params.rng is None:
+                    m = direction_numbers(D) if D else None
+                    x0 = np.zeros(D, np.uint32) if D else None
+                else:
+                    m, x0 = scramble(direction_numbers(D), td.rand_params.rng)
+                seqs.append((m, x0))
+            plan.append((gid, td, seqs))
+        # one launch for every (group, sequence) of the step
+        works, index = [], []
+        for gi, p in enumerate(plan):
+            if p is None:
+                continue
+            gid, td, seqs = p
+            start, length = rank_sub_range(td.N_samples, comm) if td.order > 0 else (0, 1)
+            for si, (m, x0) in enumerate(seqs):
+                works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
+                index.append((gi, si))
+        res = self.dev.integrate(works, precision) if works else []
+        per: Dict[int, List[np.ndarray]] = {}
+        for (gi, si), blocks in zip(index, res):
+            v = _pack_blocks(blocks)
+            if plan[gi][1].order > 0:
+                v = comm.allreduce(v)
+            per.setdefault(gi, []).append(v)
+        out = []
+        for gi, p in enumerate(plan):
+            if p is None:
+                out.append(None)
+                continue
+            vs = np.array(per[gi])
+            mean = vs.mean(axis=0)
+            std = vs.std(axis=0, ddof=1) if len(vs) > 1 else np.full(vs.shape[1], np.nan)
+            out.append((_unpack_blocks(mean, dims), _unpack_blocks(std, dims)))
+        return out
+
+
+def inchworm_step(expansion, t_i: float, t_w: float, t_f: float, top_data: Sequence[TopologiesInputData],
+                  dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm()):
+    """Regular inch step; returns (value, order_contribs, order_contribs_std) as SectorBlockMatrix."""
+    ses = _Session(dev, expansion)
+    ses.dev.set_ppgf(expansion.P)
+    return _accumulate(ses.run(_lib.QIW_GROUP_BOLD, top_data, t_i, t_w, t_f, precision, comm), top_data,
+                       expansion.dims)
+
+
+def inchworm_step_bare(expansion, t_i: float, t_f: float, top_data: Sequence[TopologiesInputData],
+                       dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm()):
+    """Initial step with bare propagators (all diagrams)."""
+    ses = _Session(dev, expansion)
+    return _accumulate(ses.run(_lib.QIW_GROUP_BARE, top_data, t_i, 0.0, t_f, precision, comm), top_data,
+                       expansion.dims)
+
+
+def _accumulate(results, top_data, dims):
+    orders = sorted({td.order for td in top_data})
+    zero = lambda: [np.zeros((d, d), np.complex128) for d in dims]
+    contribs = {o: zero() for o in orders}
+    stds = {o: zero() for o in orders}
+    for td, r in zip(top_data, results):
+        if r is None:
+            continue
+        mean, std = r
+        contribs[td.order] = [a + b for a, b in zip(contribs[td.order], mean)]
+        if td.order > 0:
+            stds[td.order] = [a + b for a, b in zip(stds[td.order], std)]
+    total = zero()
+    for o in orders:
+        total = [a + b for a, b in zip(total, contribs[o])]
+    sbm = blocks_to_sbm
+    return sbm(total), {o: sbm(v) for o, v in contribs.items()}, {o: sbm(v) for o, v in stds.items()}
+
+
+def _zero_P(expansion):
+    return [ImaginaryTimeGF(P_s.grid, P_s.norb, True) for P_s in expansion.P]
+
+
+def inchworm(expansion, orders, orders_bare, N_samples: int, n_pts_after_max: Optional[int] = None,
+             rand_params: Optional[RandomizationParams] = None, dev: Optional[Device] = None,
+             precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm(), n_steps: Optional[int] = None,
+             step_callback=None):
+    """inchworm!(expansion, grid, orders, orders_bare, N_samples; n_pts_after_max, rand_params).
+
+    Writes the bold propagator into expansion.P and returns (P_orders, P_orders_std):
+    dict order -> list of per-sector ImaginaryTimeGF.  `n_steps` stops after that many
+    regular steps (the remaining grid points keep their atomic values)."""
+    assert N_samples == 0 or (N_samples & (N_samples - 1)) == 0, "N_samples must be a power of 2"
+    rp = rand_params or RandomizationParams()
+    assert rp.N_seqs > 0
+    grid = expansion.grid
+    ses = _Session(dev, expansion)
+    orders_all = sorted(set(orders) | set(orders_bare))
+    P_orders = {o: _zero_P(expansion) for o in orders_all}
+    P_orders_std = {o: _zero_P(expansion) for o in orders_all}
+
+    top_bare = [TopologiesInputData(o, 2 * o, get_topologies_at_order(o), N_samples, rp) for o in orders_bare]
+    res = ses.run(_lib.QIW_GROUP_BARE, top_bare, grid.tau(0), 0.0, grid.tau(1), precision, comm)
+    value, contribs, stds = _accumulate(res, top_bare, expansion.dims)
+    _ppgf.set_ppgf(expansion.P, 1, value)
+    for o in contribs:
+        for s, (sf, m) in contribs[o].items():
+            P_orders[o][s].data[1] = m
+            P_orders_std[o][s].data[1] = stds[o][s][1]
+
+    top_bold = []
+    for o in orders:
+        rng = [0] if o == 0 else range(1, min(2 * o - 1, n_pts_after_max or 2 * o) + 1)
+        for npa in rng:
+            tops = get_topologies_at_order(o, npa)
+            if tops:
+                top_bold.append(TopologiesInputData(o, npa, tops, N_samples, rp))
+
+    last = grid.n_tau - 1 if n_steps is None else min(grid.n_tau - 1, 1 + n_steps)
+    for n in range(1, last):
+        ses.dev.set_ppgf(expansion.P)
+        res = ses.run(_lib.QIW_GROUP_BOLD, top_bold, grid.tau(0), grid.tau(n), grid.tau(n + 1), precision, comm)
+        value, contribs, stds = _accumulate(res, top_bold, expansion.dims)
+        _ppgf.set_ppgf(expansion.P, n + 1, value)
+        _ppgf.normalize_tau(expansion.P, n + 1)  # suppress exponential growth (src/inchworm.jl:488)
+        for o in contribs:
+            for s, (sf, m) in contribs[o].items():
+                P_orders[o][s].data[n + 1] = m
+                P_orders_std[o][s].data[n + 1] = stds[o][s][1]
+        if step_callback is not None:
+            step_callback(n)
+    return P_orders, P_orders_std
+
+
+def correlator_2p(expansion, orders, N_samples: int, rand_params: Optional[RandomizationParams] = None,
+                  dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm(),
+                  request_std: bool = False, taus: Optional[Sequence[int]] = None):
+    """correlator_2p(expansion, grid, orders, N_samples[, RequestStdDev()]).
+
+    Returns one array of <A(tau) B(0)> values on the grid per registered (A, B) pair (and the
+    standard deviations when request_std).  All tau points and groups of one correlator run
+    in a single launch: with P final, the tau points are independent."""
+    assert N_samples == 0 or (N_samples & (N_samples - 1)) == 0, "N_samples must be a power of 2"
+    rp = rand_params or RandomizationParams()
+    grid = expansion.grid
+    ses = _Session(dev, expansion)
+    ses.dev.set_ppgf(expansion.P)
+    top_data = []
+    for o in orders:
+        rng = [0] if o == 0 else range(1, 2 * o)
+        for npa in rng:
+            tops = get_topologies_at_order(o, npa, with_external_arc=True)
+            if tops:
+                top_data.append(TopologiesInputData(o, npa, tops, N_samples, rp))
+    Z = _ppgf.partition_function(expansion.P)
+    idx = list(range(grid.n_tau)) if taus is None else list(taus)
+    gs, stds = [], []
+    for c in range(len(expansion.corr_operators)):
+        A, B = expansion.corr_operators[c]
+        assert A.is_single_monomial(), "Operator A must be a single monomial in C/C^+"
+        assert B.is_single_monomial(), "Operator B must be a single monomial in C/C^+"
+        g = np.zeros(len(idx), np.complex128)
+        gstd = np.zeros(len(idx))
+        # one launch over all tau points of this correlator
+        all_tds, spans = [], []
+        for q, j in enumerate(idx):
+            tds = top_data[:1] if j == 0 else top_data
+            if j == 0 and top_data[0].order != 0:
+                tds = []
+            spans.append((q, j, len(all_tds), len(tds)))
+            all_tds += tds
+        per_tau = []
+        for (q, j, a, n) in spans:
+            per_tau.append((grid.tau(0), grid.tau(j), grid.tau(grid.n_tau - 1)))
+        works_res = _run_multi_tau(ses, all_tds, spans, per_tau, precision, comm, c)
+        for (q, j, a, n), r in zip(spans, works_res):
+            val, sd = 0j, 0.0
+            for (mean, std), td in r:
+                val += sum(np.trace(b) for b in mean)
+                if td.order > 0:
+                    sd += float(np.real(sum(np.trace(b) for b in std)))
+            g[q] = val / Z
+            gstd[q] = sd / Z.real
+        gs.append(g)
+        stds.append(gstd)
+    return (gs, stds) if request_std else gs
+
+
+def _run_multi_tau(ses: _Session, all_tds, spans, times, precision, comm, corr):
+    """Runs the correlator groups of every tau point in one qiw_integrate call."""
+    dims = ses.exp.dims
+    works, index = [], []
+    for (q, j, a, n), (t_i, t_w, t_f) in zip(spans, times):
+        for k in range(n):
+            td = all_tds[a + k]
+            if td.order > 0 and td.N_samples <= 0:
+                continue
+            gid = ses.group(_lib.QIW_GROUP_CORRELATOR, td, corr)
+            D = 2 * td.order
+            n_seqs = 1 if td.order == 0 else td.rand_params.N_seqs
+            for s in range(n_seqs):
+                if D == 0 or td.rand_params.rng is None:
+                    m, x0 = (direction_numbers(D), np.zeros(D, np.uint32)) if D else (None, None)
+                else:
+                    m, x0 = scramble(direction_numbers(D), td.rand_params.rng)
+                start, length = rank_sub_range(td.N_samples, comm) if td.order > 0 else (0, 1)
+                works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
+                index.append((q, a + k))
+    res = ses.dev.integrate(works, precision) if works else []
+    grouped: Dict[Tuple[int, int], List[np.ndarray]] = {}
+    for (q, ti), blocks in zip(index, res):
+        v = _pack_blocks(blocks)
+        if all_tds[ti].order > 0:
+            v = comm.allreduce(v)
+        grouped.setdefault((q, ti), []).append(v)
+    out = []
+    for (q, j, a, n) in spans:
+        r = []
+        for k in range(n):
+            vs = np.array(grouped.get((q, a + k), []))
+            if len(vs) == 0:
+                continue
+            mean = vs.mean(axis=0)
+            std = vs.std(axis=0, ddof=1) if len(vs) > 1 else np.full(vs.shape[1], np.nan)
+            r.append(((_unpack_blocks(mean, dims), _unpack_blocks(std, dims)), all_tds[a + k]))
+        out.append(r)
+    return out

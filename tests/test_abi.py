@@ -1,0 +1,39 @@
+"""The C-ABI library builds, loads and exports every entry point declared in include/qiw.h."""
+import ctypes as C
+import os
+import re
+
+from qiw import _lib, build
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "qiw.h")
+
+
+def declared():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(qiw_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_and_library_exports():
+    lib = C.CDLL(build.build())
+    names = declared()
+    assert set(_lib.EXPORTS) <= set(names)
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_ctx_create_reports_missing_device_without_crashing():
+    import torch
+    if torch.cuda.is_available():
+        return
+    lib = _lib.load()
+    h = C.c_void_p()
+    rc = lib.qiw_ctx_create(C.byref(h), 0)
+    assert rc == _lib.QIW_ERR_CUDA and not h.value
+
+
+def test_null_arguments_are_rejected():
+    lib = _lib.load()
+    assert lib.qiw_integrate(None, 0, None, 0, None) == _lib.QIW_ERR_ARG
+    assert lib.qiw_problem_set(None, None) == _lib.QIW_ERR_ARG
+    assert lib.qiw_last_error(None) == b"null context"

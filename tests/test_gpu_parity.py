@@ -1,0 +1,179 @@
+"""CUDA path (through the C ABI) against the CPU oracle on the same seeded inputs.
+
+Tolerance: the plain FP64 path must agree with the oracle to 1e-12 relative (max-abs error
+over the group's result blocks / max-abs of the oracle's blocks); the FP32 chain-product path
+to 1e-4.
+"""
+import numpy as np
+import pytest
+
+import oracle as orc
+from qiw import _lib, models
+from qiw.device import Work
+from qiw.diagrammatics import get_topologies_at_order
+
+pytestmark = pytest.mark.gpu
+
+REL64 = 1e-12
+REL32 = 1e-4
+
+
+def _rel(got, want):
+    scale = max(np.abs(w).max() for w in want)
+    err = max(np.abs(a - b).max() for a, b in zip(got, want))
+    return err / scale if scale > 0 else err
+
+
+def _tops(kind, order, npa):
+    if kind == _lib.QIW_GROUP_BARE:
+        return get_topologies_at_order(order)
+    if order == 0:
+        return get_topologies_at_order(0)
+    return get_topologies_at_order(order, npa, with_external_arc=(kind == _lib.QIW_GROUP_CORRELATOR))
+
+
+def _okind(kind):
+    return {_lib.QIW_GROUP_BARE: "bare", _lib.QIW_GROUP_BOLD: "bold", _lib.QIW_GROUP_CORRELATOR: "corr"}[kind]
+
+
+CASES = [
+    ("anderson", _lib.QIW_GROUP_BARE, 2, 0), ("anderson", _lib.QIW_GROUP_BARE, 4, 0),
+    ("anderson", _lib.QIW_GROUP_BOLD, 0, 0), ("anderson", _lib.QIW_GROUP_BOLD, 1, 1),
+    ("anderson", _lib.QIW_GROUP_BOLD, 3, 2), ("anderson", _lib.QIW_GROUP_BOLD, 4, 4),
+    ("anderson", _lib.QIW_GROUP_CORRELATOR, 2, 1), ("anderson", _lib.QIW_GROUP_CORRELATOR, 3, 5),
+    ("eg", _lib.QIW_GROUP_BARE, 2, 0), ("eg", _lib.QIW_GROUP_BOLD, 2, 2), ("eg", _lib.QIW_GROUP_BOLD, 3, 3),
+    ("single", _lib.QIW_GROUP_BOLD, 3, 1),
+]
+
+
+def _model(name):
+    if name == "anderson":
+        return models.anderson(n_tau=40, corr=True)
+    if name == "eg":
+        return models.eg_discrete_bath(n_tau=40)
+    return models.single_level(n_tau=20, spline=True)
+
+
+@pytest.mark.parametrize("name,kind,order,npa", CASES)
+def test_group_fp64_matches_oracle(device, name, kind, order, npa):
+    exp = _model(name)
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    tops = _tops(kind, order, npa)
+    corr = 0 if kind == _lib.QIW_GROUP_CORRELATOR else None
+    gid = device.create_group(kind, order, npa, tops, corr)
+    if kind == _lib.QIW_GROUP_BARE:
+        t = (g.tau(0), 0.0, g.tau(1))
+    elif kind == _lib.QIW_GROUP_BOLD:
+        t = (g.tau(0), g.tau(17), g.tau(18))
+    else:
+        t = (g.tau(0), g.tau(9), g.tau(g.n_tau - 1))
+    N = 128
+    got = device.integrate([Work(gid, *t, 0, N, N)])[0]
+    want = orc.OracleProblem(exp).integrate(_okind(kind), order, npa, [(x.pairs, x.parity) for x in tops],
+                                            *t, N, corr=corr)
+    assert _rel(got, want) < REL64
+    got32 = device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32)[0]
+    assert _rel(got32, want) < REL32
+
+
+def test_ragged_ranges_and_rank_split(device):
+    exp = models.anderson(n_tau=30)
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    tops = get_topologies_at_order(3, 3)
+    gid = device.create_group(_lib.QIW_GROUP_BOLD, 3, 3, tops)
+    t = (g.tau(0), g.tau(10), g.tau(11))
+    ob = orc.OracleProblem(exp)
+    tl = [(x.pairs, x.parity) for x in tops]
+    for N in (1, 3, 100, 257):
+        got = device.integrate([Work(gid, *t, 0, N, N)])[0]
+        assert _rel(got, ob.integrate("bold", 3, 3, tl, *t, N)) < REL64
+    # three "ranks" with rank_sub_range chunks, one launch, summed like all_reduce!
+    N = 512
+    chunks = [171, 171, 170]
+    starts = [0, 171, 342]
+    parts = device.integrate([Work(gid, *t, s, c, N) for s, c in zip(starts, chunks)])
+    tot = [sum(p[s] for p in parts) for s in range(len(parts[0]))]
+    assert _rel(tot, ob.integrate("bold", 3, 3, tl, *t, N, n_ranks=3)) < REL64
+
+
+def test_zero_samples_and_errors(device):
+    exp = models.anderson(n_tau=16)
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    gid = device.create_group(_lib.QIW_GROUP_BOLD, 1, 1, get_topologies_at_order(1, 1))
+    g = exp.grid
+    got = device.integrate([Work(gid, g.tau(0), g.tau(3), g.tau(4), 0, 0, 16)])[0]
+    assert all(np.all(b == 0) for b in got)
+    with pytest.raises(_lib.QiwError) as ei:
+        device.integrate([Work(gid + 1000, 0.0, 0.1, 0.2, 0, 8, 8)])
+    assert ei.value.code == _lib.QIW_ERR_ARG
+    with pytest.raises(_lib.QiwError):
+        device.integrate([Work(gid, 0.5, 0.1, 0.2, 0, 8, 8)])   # t_i > t_w
+
+
+def test_complex_phase_input_is_rejected(device):
+    exp = models.anderson(n_tau=16)
+    device.set_problem(exp)
+    P = [p.copy() for p in exp.P]
+    P[0].data = P[0].data + 1e-3   # real part: not of the imaginary-branch form -i * real
+    device.set_ppgf(P)
+    gid = device.create_group(_lib.QIW_GROUP_BOLD, 1, 1, get_topologies_at_order(1, 1))
+    with pytest.raises(_lib.QiwError) as ei:
+        device.integrate([Work(gid, 0.0, 1.0, 1.5, 0, 8, 8)])
+    assert ei.value.code == _lib.QIW_ERR_UNSUPPORTED
+
+
+def test_rerun_is_bit_identical(device):
+    exp = models.eg_discrete_bath(n_tau=32)
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    gid = device.create_group(_lib.QIW_GROUP_BOLD, 3, 2, get_topologies_at_order(3, 2))
+    w = [Work(gid, g.tau(0), g.tau(12), g.tau(13), 0, 1000, 1024)]
+    a = device.integrate(w)[0]
+    b = device.integrate(w)[0]
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+def test_inchworm_loop_matches_oracle(device):
+    from qiw.inchworm import inchworm
+    exp = models.anderson(n_tau=24)
+    exp_o = models.anderson(n_tau=24)
+    inchworm(exp, range(0, 4), range(0, 4), 64, dev=device)
+    pb = orc.inchworm(exp_o, range(0, 4), range(0, 4), 64)
+    for s in range(len(exp.P)):
+        a, b = exp.P[s].data, pb.P_data[s]
+        assert np.abs(a - b).max() <= 1e-11 * np.abs(b).max()
+
+
+def test_golden_inchworm_h5_through_gpu(device):
+    """The reference's own fixture (test/inchworm.h5, test/inchworm.jl:180-212) on the GPU path."""
+    import json, os
+    from qiw import operators as op
+    from qiw.inchworm import inchworm, correlator_2p
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "inchworm_h5.json")))
+    exp = models.single_level()
+    inchworm(exp, range(0, 4), range(0, 3), 2 ** 8, dev=device)
+    for s in range(2):
+        want = np.array(gold["P"][s]["re"]) + 1j * np.array(gold["P"][s]["im"])
+        got = exp.P[s].data[:, 0, 0]
+        assert np.linalg.norm(got - want) <= 5e-8 * np.linalg.norm(want)
+    exp.add_corr_operators((op.c("0"), op.c_dag("0")))
+    g = -correlator_2p(exp, range(0, 4), 2 ** 8, dev=device)[0]
+    want = np.array(gold["g"]["re"]) + 1j * np.array(gold["g"]["im"])
+    assert np.linalg.norm(g - want) <= 1e-6 * np.linalg.norm(want)
+
+
+def test_correlator_matches_oracle(device):
+    from qiw.inchworm import correlator_2p
+    exp = models.anderson(n_tau=20, corr=True)
+    device.set_problem(exp)
+    got = correlator_2p(exp, range(0, 3), 64, dev=device)
+    pb = orc.OracleProblem(exp)
+    want = orc.correlator_2p(pb, range(0, 3), 64)
+    for a, b in zip(got, want):
+        assert np.abs(a - b).max() <= 1e-11 * np.abs(b).max()

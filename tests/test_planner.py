@@ -1,0 +1,105 @@
+"""The host planner's merged-DAG programs, executed on the CPU, against the oracle's
+reference-style tree traversal (no GPU involved)."""
+import numpy as np
+import pytest
+
+import oracle as orc
+import planexec as pe
+from qiw import _lib, models
+from qiw.diagrammatics import get_topologies_at_order
+
+REL = 1e-13
+
+
+def _case(exp, kind, order, npa, times, N, budget=8192, corr=None):
+    pk = _lib.PackedProblem(exp)
+    ob = orc.OracleProblem(exp)
+    if kind == _lib.QIW_GROUP_BARE:
+        tops, okind = get_topologies_at_order(order), "bare"
+    elif kind == _lib.QIW_GROUP_BOLD:
+        tops, okind = get_topologies_at_order(order, npa if order else None), "bold"
+    else:
+        tops = get_topologies_at_order(order, npa, with_external_arc=True) if order else get_topologies_at_order(0)
+        okind = "corr"
+    hp = pe.HostPlan(pk, kind, order, npa, tops, corr=pk.corr_ops[corr] if corr is not None else None,
+                     arena_budget=budget)
+    got = pe.execute(hp, exp, pk, pe.p_tables(exp), *times, N)
+    want = ob.integrate(okind, order, npa, [(t.pairs, t.parity) for t in tops], *times, N, corr=corr)
+    scale = max(np.abs(w).max() for w in want)
+    err = max(np.abs(a - b).max() for a, b in zip(got, want))
+    return (err / scale if scale > 0 else err), hp
+
+
+@pytest.mark.parametrize("kind,order,npa", [
+    (_lib.QIW_GROUP_BARE, 1, 0), (_lib.QIW_GROUP_BARE, 3, 0),
+    (_lib.QIW_GROUP_BOLD, 0, 0), (_lib.QIW_GROUP_BOLD, 1, 1), (_lib.QIW_GROUP_BOLD, 2, 3),
+    (_lib.QIW_GROUP_BOLD, 3, 3), (_lib.QIW_GROUP_BOLD, 4, 1), (_lib.QIW_GROUP_BOLD, 4, 7),
+])
+def test_anderson_groups(kind, order, npa):
+    exp = models.anderson(n_tau=30)
+    g = exp.grid
+    times = (g.tau(0), 0.0, g.tau(1)) if kind == _lib.QIW_GROUP_BARE else (g.tau(0), g.tau(11), g.tau(12))
+    rel, hp = _case(exp, kind, order, npa, times, 64)
+    assert rel < REL
+    assert hp.flops < hp.tree_flops
+
+
+@pytest.mark.parametrize("kind,order,npa", [
+    (_lib.QIW_GROUP_BARE, 2, 0), (_lib.QIW_GROUP_BOLD, 2, 2), (_lib.QIW_GROUP_BOLD, 3, 1),
+])
+def test_eg_groups(kind, order, npa):
+    exp = models.eg_discrete_bath(n_tau=24)
+    g = exp.grid
+    times = (g.tau(0), 0.0, g.tau(1)) if kind == _lib.QIW_GROUP_BARE else (g.tau(0), g.tau(9), g.tau(10))
+    rel, _ = _case(exp, kind, order, npa, times, 16)
+    assert rel < REL
+
+
+@pytest.mark.parametrize("order,npa", [(0, 0), (1, 1), (2, 1), (3, 4)])
+def test_correlator_groups(order, npa):
+    exp = models.anderson(n_tau=30, corr=True)
+    g = exp.grid
+    for c in range(3):
+        rel, _ = _case(exp, _lib.QIW_GROUP_CORRELATOR, order, npa, (g.tau(0), g.tau(13), g.tau(29)), 32, corr=c)
+        assert rel < REL
+
+
+def test_spline_delta_group():
+    exp = models.single_level(n_tau=20, spline=True)
+    g = exp.grid
+    rel, _ = _case(exp, _lib.QIW_GROUP_BOLD, 3, 2, (g.tau(0), g.tau(7), g.tau(8)), 64)
+    assert rel < REL
+
+
+def test_budget_split_gives_same_result():
+    """A tight working-set budget splits the roots into batches (less merging) -- same sum."""
+    exp = models.eg_discrete_bath(n_tau=24)
+    g = exp.grid
+    t = (g.tau(0), g.tau(9), g.tau(10))
+    rel_a, hp_a = _case(exp, _lib.QIW_GROUP_BOLD, 3, 3, t, 8, budget=8192)
+    budget = hp_a.arena // 2
+    rel_b, hp_b = _case(exp, _lib.QIW_GROUP_BOLD, 3, 3, t, 8, budget=budget)
+    assert rel_a < REL and rel_b < REL
+    assert hp_b.batches > hp_a.batches
+    assert hp_b.arena <= budget < hp_a.arena
+
+
+def test_offdiagonal_leaf_is_reported():
+    """A block off-diagonal leaf raises, like the reference's assertion (topology_eval.jl:462)."""
+    from qiw import operators as op
+    from qiw.ed import EDCore
+    from qiw.expansion import Expansion, InteractionPair
+    from qiw.gf import ImaginaryTimeGrid, DeltaDOS, gf_from_dos, ph_conj
+    H = 0.3 * op.n("a") - 0.2 * op.n("b")
+    soi = op.SetOfIndices([["a"], ["b"]])
+    ed = EDCore(H, soi)
+    grid = ImaginaryTimeGrid(5.0, 8)
+    D = gf_from_dos(DeltaDOS.make([0.1]), grid)
+    # a pair moving an electron a -> b: sectors do not close on themselves
+    exp = Expansion(ed, grid, [InteractionPair(op.c_dag("b"), op.c("a"), D),
+                               InteractionPair(op.c("a"), op.c_dag("b"), ph_conj(D))])
+    pk = _lib.PackedProblem(exp)
+    tops = get_topologies_at_order(1, 1)
+    with pytest.raises(_lib.QiwError) as ei:
+        pe.HostPlan(pk, _lib.QIW_GROUP_BOLD, 1, 1, tops)
+    assert ei.value.code == _lib.QIW_ERR_OFFDIAG
