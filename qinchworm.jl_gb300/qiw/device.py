@@ -91,7 +91,7 @@ class Device:
         descs = (_lib.WorkDesc * len(works))()
         keep = []
         for i, w in enumerate(works):
-            order = self.group_info[w.group][1]
+            order = self.group_info.get(w.group, (0, 0, 0))[1]
             D = 2 * order
             m = w.sobol_m if w.sobol_m is not None else (self.sobol(D) if D else np.zeros((1, 32), np.uint32))
             x0 = w.sobol_x0 if w.sobol_x0 is not None else np.zeros(max(D, 1), np.uint32)

@@ -96,9 +96,11 @@ class _Session:
 
     def __init__(self, dev: Optional[Device], expansion):
         self.dev = dev if dev is not None else Device(0)
-        if getattr(self.dev, "_expansion", None) is not expansion:
+        key = (id(expansion), len(expansion.corr_operators), len(expansion.pairs))
+        if getattr(self.dev, "_expansion", None) is not expansion or getattr(self.dev, "_problem_key", None) != key:
             self.dev.set_problem(expansion)
             self.dev._expansion = expansion
+            self.dev._problem_key = key
             self.dev._groups = {}
         self.exp = expansion
 
