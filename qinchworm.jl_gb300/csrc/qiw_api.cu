@@ -47,6 +47,7 @@ struct GroupRec {
   DevBuf<PmJob> pm;
   DevBuf<WJob> wj;
   DevBuf<Instr> ins;
+  DevBuf<int32_t> batch;
   DevGroup dg;
 };
 
@@ -109,7 +110,7 @@ struct qiw_ctx {
   bool groups_dirty = true;
 
   DevBuf<DevWork> d_works;
-  DevBuf<int2> d_cta_map;
+  DevBuf<int4> d_cta_map;
   DevBuf<double> d_partials, d_out;
   DevBuf<int> d_cta_first, d_res_sizes, d_out_off, d_err;
   DevBuf<uint32_t> d_sobol;
@@ -129,6 +130,7 @@ struct qiw_ctx {
       g->pm.release();
       g->wj.release();
       g->ins.release();
+      g->batch.release();
       delete g;
     }
     groups.clear();
@@ -338,6 +340,7 @@ int qiw_group_create(qiw_ctx *c, const qiw_group_desc *d, int32_t *group_id) {
   if ((rc = c->cuda(g->pm.upload(p.pm.data(), p.pm.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(g->wj.upload(p.wj.data(), p.wj.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(g->ins.upload(p.ins.data(), p.ins.size(), c->stream), "upload plan")) ||
+      (rc = c->cuda(g->batch.upload(p.batch_begin.data(), p.batch_begin.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(cudaStreamSynchronize(c->stream), "upload plan"))) {
     delete g;
     return rc;
@@ -362,9 +365,11 @@ int qiw_group_create(qiw_ctx *c, const qiw_group_desc *d, int32_t *group_id) {
   dg.n_instr = (int)p.ins.size();
   dg.arena = (int)p.arena;
   dg.res_size = p.res_size;
+  dg.n_batches = (int)p.batch_begin.size() - 1;
   dg.pm = g->pm.p;
   dg.wj = g->wj.p;
   dg.ins = g->ins.p;
+  dg.batch_begin = g->batch.p;
   c->groups.push_back(g);
   c->groups_dirty = true;
   *group_id = (int32_t)c->groups.size() - 1;
@@ -391,7 +396,7 @@ int qiw_integrate(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t
   if (n_work == 0) return QIW_OK;
   bool need_P = false;
   std::vector<DevWork> works(n_work);
-  std::vector<int2> cta_map;
+  std::vector<int4> cta_map;
   std::vector<int> cta_first(n_work), res_sizes(n_work), out_off(n_work);
   std::vector<uint32_t> sob;
   int64_t arena_max = 0;
@@ -424,9 +429,18 @@ int qiw_integrate(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t
                      : simplex_volume(p.d_before, wd.t_w - wd.t_i) * simplex_volume(p.d_after, wd.t_f - wd.t_w);
       w.scale = J / (double)wd.n_total;
     }
-    w.n_cta = (int)((w.n_samples + threads - 1) / threads);
+    const int n_tiles = (int)((w.n_samples + threads - 1) / threads);
+    const int n_b = std::max(0, (int)p.batch_begin.size() - 1);
+    w.n_cta = n_tiles * n_b;
     cta_first[i] = (int)cta_map.size();
-    for (int k = 0; k < w.n_cta; ++k) cta_map.push_back(make_int2(i, k * threads));
+    // heaviest batches first within the work item: the block scheduler then starts the
+    // long CTAs early (the finish kernel sums the partials in this same fixed order)
+    std::vector<int> order(n_b);
+    for (int b = 0; b < n_b; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return p.batch_flops[x] > p.batch_flops[y]; });
+    for (int b : order)
+      for (int k = 0; k < n_tiles; ++k) cta_map.push_back(make_int4(i, b, k * threads, 0));
     res_sizes[i] = p.res_size;
     out_off[i] = out_total;
     out_total += p.res_size;

@@ -60,10 +60,11 @@ struct DevGroup {
   int32_t n_pm, n_w, n_instr;
   int32_t arena;               // elements of the compute type
   int32_t res_size;            // sum d^2 (result elements)
-  int32_t pad;
+  int32_t n_batches;           // independent instruction ranges (one per initial sector or split)
   const PmJob *pm;
   const WJob *wj;
   const Instr *ins;
+  const int32_t *batch_begin;  // [n_batches + 1]
 };
 
 struct DevWork {

@@ -54,14 +54,220 @@ __device__ __forceinline__ void lin_index(double dt, double inv_h, int n_tau, in
   *f = x - (double)k;
 }
 
+
+// ---------------------------------------------------------------------------------------
+// Matrix instructions.  Block dimensions 1, 2 and 4 (every sector of the Anderson and eg
+// models) take fully unrolled paths: all operands are loaded into registers first, so the
+// arena reads of one instruction are in flight together, then 4..64 independent FMAs run.
+// Other dimensions use the generic loops.
+
+__device__ __forceinline__ int dcode(int d) { return d == 1 ? 0 : d == 2 ? 1 : d == 4 ? 2 : -1; }
+
+template <typename T, int R, int C>
+__device__ __forceinline__ void pmul_u(T *A, int dst, int pm, int src) {
+  T p[R * R], x[R * C];
+#pragma unroll
+  for (int i = 0; i < R * R; ++i) p[i] = A[pm + i];
+#pragma unroll
+  for (int i = 0; i < R * C; ++i) x[i] = A[src + i];
+#pragma unroll
+  for (int j = 0; j < C; ++j)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      T acc = p[r] * x[j * R];
+#pragma unroll
+      for (int k = 1; k < R; ++k) acc = fmaT<T>(p[k * R + r], x[j * R + k], acc);
+      A[dst + j * R + r] = acc;
+    }
+}
+
+template <typename T, int R, int C>
+__device__ __forceinline__ void pmuld_u(T *A, int dst, int pm, int src) {
+  T p[R], x[R * C];
+#pragma unroll
+  for (int i = 0; i < R; ++i) p[i] = A[pm + i];
+#pragma unroll
+  for (int i = 0; i < R * C; ++i) x[i] = A[src + i];
+#pragma unroll
+  for (int j = 0; j < C; ++j)
+#pragma unroll
+    for (int r = 0; r < R; ++r) A[dst + j * R + r] = p[r] * x[j * R + r];
+}
+
+template <typename T, int R, int K, int C>
+__device__ __forceinline__ void omul_u(T *A, const T *O, int dst, int oa, int src, T coef, bool accf) {
+  T o[R * K], x[K * C], y[R * C];
+#pragma unroll
+  for (int i = 0; i < R * K; ++i) o[i] = __ldg(O + oa + i);
+#pragma unroll
+  for (int i = 0; i < K * C; ++i) x[i] = A[src + i];
+  if (accf) {
+#pragma unroll
+    for (int i = 0; i < R * C; ++i) y[i] = A[dst + i];
+  }
+#pragma unroll
+  for (int j = 0; j < C; ++j)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      T acc = o[r] * x[j * K];
+#pragma unroll
+      for (int k = 1; k < K; ++k) acc = fmaT<T>(o[k * R + r], x[j * K + k], acc);
+      A[dst + j * R + r] = accf ? fmaT<T>(coef, acc, y[j * R + r]) : coef * acc;
+    }
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void axpy_u(T *A, int dst, int src, T coef, bool accf) {
+  T x[N], y[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) x[i] = A[src + i];
+  if (accf) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) y[i] = A[dst + i];
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) A[dst + i] = accf ? fmaT<T>(coef, x[i], y[i]) : coef * x[i];
+}
+
+#define QIW_D3(F, ...)                                                                            \
+  switch (code) {                                                                                 \
+    case 0: F<T, 1, 1, 1>(__VA_ARGS__); break;  case 1: F<T, 1, 1, 2>(__VA_ARGS__); break;        \
+    case 2: F<T, 1, 1, 4>(__VA_ARGS__); break;  case 3: F<T, 1, 2, 1>(__VA_ARGS__); break;        \
+    case 4: F<T, 1, 2, 2>(__VA_ARGS__); break;  case 5: F<T, 1, 2, 4>(__VA_ARGS__); break;        \
+    case 6: F<T, 1, 4, 1>(__VA_ARGS__); break;  case 7: F<T, 1, 4, 2>(__VA_ARGS__); break;        \
+    case 8: F<T, 1, 4, 4>(__VA_ARGS__); break;  case 9: F<T, 2, 1, 1>(__VA_ARGS__); break;        \
+    case 10: F<T, 2, 1, 2>(__VA_ARGS__); break; case 11: F<T, 2, 1, 4>(__VA_ARGS__); break;       \
+    case 12: F<T, 2, 2, 1>(__VA_ARGS__); break; case 13: F<T, 2, 2, 2>(__VA_ARGS__); break;       \
+    case 14: F<T, 2, 2, 4>(__VA_ARGS__); break; case 15: F<T, 2, 4, 1>(__VA_ARGS__); break;       \
+    case 16: F<T, 2, 4, 2>(__VA_ARGS__); break; case 17: F<T, 2, 4, 4>(__VA_ARGS__); break;       \
+    case 18: F<T, 4, 1, 1>(__VA_ARGS__); break; case 19: F<T, 4, 1, 2>(__VA_ARGS__); break;       \
+    case 20: F<T, 4, 1, 4>(__VA_ARGS__); break; case 21: F<T, 4, 2, 1>(__VA_ARGS__); break;       \
+    case 22: F<T, 4, 2, 2>(__VA_ARGS__); break; case 23: F<T, 4, 2, 4>(__VA_ARGS__); break;       \
+    case 24: F<T, 4, 4, 1>(__VA_ARGS__); break; case 25: F<T, 4, 4, 2>(__VA_ARGS__); break;       \
+    default: F<T, 4, 4, 4>(__VA_ARGS__); break;                                                   \
+  }
+
+#define QIW_D2(F, ...)                                                                            \
+  switch (code) {                                                                                 \
+    case 0: F<T, 1, 1>(__VA_ARGS__); break; case 1: F<T, 1, 2>(__VA_ARGS__); break;               \
+    case 2: F<T, 1, 4>(__VA_ARGS__); break; case 3: F<T, 2, 1>(__VA_ARGS__); break;               \
+    case 4: F<T, 2, 2>(__VA_ARGS__); break; case 5: F<T, 2, 4>(__VA_ARGS__); break;               \
+    case 6: F<T, 4, 1>(__VA_ARGS__); break; case 7: F<T, 4, 2>(__VA_ARGS__); break;               \
+    default: F<T, 4, 4>(__VA_ARGS__); break;                                                      \
+  }
+
+template <typename T, int RESMAX>
+__device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, double *R) {
+  const int rows = I.rows, cols = I.cols;
+  switch (I.op) {
+    case OP_LOADP: {
+      const T c = (T)I.c;
+      if (I.inner) {
+#pragma unroll 1
+        for (int j = 0; j < rows; ++j)
+#pragma unroll 1
+          for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = (r == j) ? c * A[I.a + r] : (T)0;
+      } else {
+#pragma unroll 1
+        for (int e = 0; e < rows * rows; ++e) A[I.dst + e] = c * A[I.a + e];
+      }
+      break;
+    }
+    case OP_LOADC: {
+      const T c = (T)I.c;
+#pragma unroll 1
+      for (int e = 0; e < rows * cols; ++e) A[I.dst + e] = c * __ldg(O + I.a + e);
+      break;
+    }
+    case OP_PMUL: {
+      const int cr = dcode(rows), cc = dcode(cols);
+      if (cr >= 0 && cc >= 0) {
+        const int code = cr * 3 + cc;
+        QIW_D2(pmul_u, A, I.dst, I.a, I.src)
+      } else {
+#pragma unroll 1
+        for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+          for (int r = 0; r < rows; ++r) {
+            T acc = (T)0;
+#pragma unroll 4
+            for (int k = 0; k < rows; ++k) acc = fmaT<T>(A[I.a + k * rows + r], A[I.src + j * rows + k], acc);
+            A[I.dst + j * rows + r] = acc;
+          }
+      }
+      break;
+    }
+    case OP_PMULD: {
+      const int cr = dcode(rows), cc = dcode(cols);
+      if (cr >= 0 && cc >= 0) {
+        const int code = cr * 3 + cc;
+        QIW_D2(pmuld_u, A, I.dst, I.a, I.src)
+      } else {
+#pragma unroll 1
+        for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+          for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = A[I.a + r] * A[I.src + j * rows + r];
+      }
+      break;
+    }
+    case OP_OMUL: {
+      const int inner = I.inner;
+      const T coef = (I.w >= 0) ? (T)I.c * A[I.w] : (T)I.c;
+      const int cr = dcode(rows), ck = dcode(inner), cc = dcode(cols);
+      if (cr >= 0 && ck >= 0 && cc >= 0) {
+        const int code = cr * 9 + ck * 3 + cc;
+        QIW_D3(omul_u, A, O, I.dst, I.a, I.src, coef, I.acc != 0)
+      } else {
+#pragma unroll 1
+        for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+          for (int r = 0; r < rows; ++r) {
+            T acc = (T)0;
+#pragma unroll 4
+            for (int k = 0; k < inner; ++k) acc = fmaT<T>(__ldg(O + I.a + k * rows + r), A[I.src + j * inner + k], acc);
+            const int o = I.dst + j * rows + r;
+            A[o] = I.acc ? fmaT<T>(coef, acc, A[o]) : coef * acc;
+          }
+      }
+      break;
+    }
+    case OP_AXPY: {
+      const T coef = (I.w >= 0) ? (T)I.c * A[I.w] : (T)I.c;
+      const int n = rows * cols;
+      const bool accf = I.acc != 0;
+      switch (n) {
+        case 1: axpy_u<T, 1>(A, I.dst, I.src, coef, accf); break;
+        case 2: axpy_u<T, 2>(A, I.dst, I.src, coef, accf); break;
+        case 4: axpy_u<T, 4>(A, I.dst, I.src, coef, accf); break;
+        case 8: axpy_u<T, 8>(A, I.dst, I.src, coef, accf); break;
+        case 16: axpy_u<T, 16>(A, I.dst, I.src, coef, accf); break;
+        default:
+#pragma unroll 1
+          for (int e = 0; e < n; ++e) {
+            const int o = I.dst + e;
+            A[o] = accf ? fmaT<T>(coef, A[I.src + e], A[o]) : coef * A[I.src + e];
+          }
+      }
+      break;
+    }
+    case OP_LEAF: {
+#pragma unroll 1
+      for (int e = 0; e < rows * cols; ++e) R[I.a + e] += (double)A[I.src + e];
+      break;
+    }
+    default:
+      break;
+  }
+}
+
 template <typename T, int ARENA, int RESMAX>
 __global__ void __launch_bounds__(kMaxThreads)
     eval_kernel(DevProblem pb, const DevGroup *__restrict__ groups, const DevWork *__restrict__ works,
-                const int2 *__restrict__ cta_map, double *__restrict__ partials) {
-  const int2 cm = cta_map[blockIdx.x];
+                const int4 *__restrict__ cta_map, double *__restrict__ partials) {
+  const int4 cm = cta_map[blockIdx.x];   // (work item, batch, first sample of the tile, -)
   const DevWork &w = works[cm.x];
   const DevGroup &g = groups[w.group];
-  const uint64_t sidx = (uint64_t)cm.y + threadIdx.x;
+  const uint64_t sidx = (uint64_t)cm.z + threadIdx.x;
   const bool active = sidx < w.n_samples;
   const int res_size = g.res_size;
 
@@ -176,84 +382,13 @@ __global__ void __launch_bounds__(kMaxThreads)
       A[job.off] = val;
     }
 
-    // The group's program.
+    // The group's program: instructions of this CTA's batch.
     const T *O = reinterpret_cast<const T *>(pb.opv);
-    const int n_ins = g.n_instr;
+    const int i0 = __ldg(g.batch_begin + cm.y), i1 = __ldg(g.batch_begin + cm.y + 1);
 #pragma unroll 1
-    for (int ip = 0; ip < n_ins; ++ip) {
+    for (int ip = i0; ip < i1; ++ip) {
       const Instr I = load_instr(g.ins + ip);
-      const int rows = I.rows, cols = I.cols;
-      switch (I.op) {
-        case OP_LOADP: {
-          const T c = (T)I.c;
-          if (I.inner) {
-#pragma unroll 1
-            for (int j = 0; j < rows; ++j)
-#pragma unroll 1
-              for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = (r == j) ? c * A[I.a + r] : (T)0;
-          } else {
-#pragma unroll 1
-            for (int e = 0; e < rows * rows; ++e) A[I.dst + e] = c * A[I.a + e];
-          }
-          break;
-        }
-        case OP_LOADC: {
-          const T c = (T)I.c;
-#pragma unroll 1
-          for (int e = 0; e < rows * cols; ++e) A[I.dst + e] = c * __ldg(O + I.a + e);
-          break;
-        }
-        case OP_PMUL: {
-#pragma unroll 1
-          for (int j = 0; j < cols; ++j)
-#pragma unroll 1
-            for (int r = 0; r < rows; ++r) {
-              T acc = (T)0;
-#pragma unroll 1
-              for (int k = 0; k < rows; ++k) acc = fmaT<T>(A[I.a + k * rows + r], A[I.src + j * rows + k], acc);
-              A[I.dst + j * rows + r] = acc;
-            }
-          break;
-        }
-        case OP_PMULD: {
-#pragma unroll 1
-          for (int j = 0; j < cols; ++j)
-#pragma unroll 1
-            for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = A[I.a + r] * A[I.src + j * rows + r];
-          break;
-        }
-        case OP_OMUL: {
-          const int inner = I.inner;
-          const T coef = (I.w >= 0) ? (T)I.c * A[I.w] : (T)I.c;
-#pragma unroll 1
-          for (int j = 0; j < cols; ++j)
-#pragma unroll 1
-            for (int r = 0; r < rows; ++r) {
-              T acc = (T)0;
-#pragma unroll 1
-              for (int k = 0; k < inner; ++k) acc = fmaT<T>(__ldg(O + I.a + k * rows + r), A[I.src + j * inner + k], acc);
-              const int o = I.dst + j * rows + r;
-              A[o] = I.acc ? fmaT<T>(coef, acc, A[o]) : coef * acc;
-            }
-          break;
-        }
-        case OP_AXPY: {
-          const T coef = (I.w >= 0) ? (T)I.c * A[I.w] : (T)I.c;
-#pragma unroll 1
-          for (int e = 0; e < rows * cols; ++e) {
-            const int o = I.dst + e;
-            A[o] = I.acc ? fmaT<T>(coef, A[I.src + e], A[o]) : coef * A[I.src + e];
-          }
-          break;
-        }
-        case OP_LEAF: {
-#pragma unroll 1
-          for (int e = 0; e < rows * cols; ++e) R[I.a + e] += (double)A[I.src + e];
-          break;
-        }
-        default:
-          break;
-      }
+      exec_instr<T, RESMAX>(I, A, O, R);
     }
   }
 

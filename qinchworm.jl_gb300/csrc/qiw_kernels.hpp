@@ -18,7 +18,7 @@ struct LaunchArgs {
   DevProblem pb;
   const DevGroup *groups;
   const DevWork *works;
-  const int2 *cta_map;
+  const int4 *cta_map;
   double *partials;
   int n_cta, threads;
   int64_t arena_max;

@@ -604,9 +604,11 @@ int plan_group(const HostProblem &pb, const GroupSpec &g, const PlanOptions &opt
   int64_t fixed_bound = (int64_t)(out->n_nodes - 1) * sumd2 + (int64_t)arcs.size() * pb.n_pairs;
   int64_t dyn_budget = std::max<int64_t>(opt.arena_budget - fixed_bound, 64);
 
-  std::vector<std::pair<int, int>> all_roots;
+  // One root list per initial sector: different s0 never merge, so each s0 is an
+  // independent batch (a separately schedulable unit of work) at no extra cost.
+  std::vector<std::vector<std::pair<int, int>>> s0_roots(pb.S);
   for (int t = 0; t < (int)g.tops.size(); ++t)
-    for (int s0 = 0; s0 < pb.S; ++s0) all_roots.emplace_back(t, s0);
+    for (int s0 = 0; s0 < pb.S; ++s0) s0_roots[s0].emplace_back(t, s0);
 
   std::vector<Instr> ins;
   int64_t dyn_peak = 0;
@@ -652,14 +654,20 @@ int plan_group(const HostProblem &pb, const GroupSpec &g, const PlanOptions &opt
       return QIW_ERR_MEMORY;
     }
     for (auto &nd : nodes) dag_nodes += nd.alive ? 1 : 0;
+    if (bi.empty()) return 0;
+    out->batch_begin.push_back((int32_t)ins.size());
+    out->batch_flops.push_back(fl);
     ins.insert(ins.end(), bi.begin(), bi.end());
     dyn_peak = std::max(dyn_peak, peak);
     flops += fl;
     n_batches++;
     return 0;
   };
-  rc = plan_roots(all_roots);
-  if (rc) return rc;
+  for (int s0 = 0; s0 < pb.S; ++s0) {
+    rc = plan_roots(s0_roots[s0]);
+    if (rc) return rc;
+  }
+  out->batch_begin.push_back((int32_t)ins.size());
 
   // Resolve arena offsets: [Pm jobs][W jobs][dynamic].
   int64_t off = 0;

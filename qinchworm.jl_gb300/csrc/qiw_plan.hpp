@@ -52,6 +52,8 @@ struct Plan {
   double tree_flops = 0.0;       // per sample, reference tree (complex arithmetic)
   int64_t tree_leaves = 0;
   int n_batches = 0;
+  std::vector<int32_t> batch_begin;   // instruction index of each batch start, + end sentinel
+  std::vector<double> batch_flops;    // flops per sample of each batch
 };
 
 // Returns 0 on success, a QIW_ERR_* code otherwise (message in *err).
