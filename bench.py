@@ -257,7 +257,8 @@ def run_ours(args):
     d2h = len(tds) * S2 * 16 + 4
     if rank != 0:
         return
-    peak = fp64_peak_tflops() if args.precision == "fp64" else None
+    peak = dev.fma_peak_tflops(prec)
+    dgemm = fp64_peak_tflops() if args.precision == "fp64" else None
     achieved = flops_rank * args.steps / k_tot / 1e12
     line = {
         "metric": METRIC if args.precision == "fp64" else METRIC.replace("plain FP64", "FP32 chain products"),
@@ -269,10 +270,11 @@ def run_ours(args):
                    "topologies_per_step": sum(len(td.topologies) for td in tds), "l2": "256 MB write between timed steps"},
         "e2e": {"value": units / w_tot, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * w_tot / args.steps},
-        "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": (achieved / peak) if peak else None, "traffic": None,
-                     "peak_source": "measured cuBLAS DGEMM 4096^3 on this GPU (no FP64 entry in MEASURED_PEAKS.json)",
-                     "flops_per_step": flops_rank},
+        "roofline": {"bound": "fp64_pipe" if args.precision == "fp64" else "fp32_pipe", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": None,
+                     "peak_source": "measured on this GPU: independent FMA chains on every SM (qiw_measure_fma_peak); "
+                                    "MEASURED_PEAKS.json has no FP64 or FP32 CUDA-core entry",
+                     "dgemm_tflops_measured": dgemm, "flops_per_step": flops_rank},
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,
     }

@@ -140,6 +140,11 @@ int qiw_integrate(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, int32
 /* Kernel time of the most recent qiw_integrate (ms, CUDA events on the context stream). */
 double qiw_last_kernel_ms(const qiw_ctx *ctx);
 
+/* No counterpart in the reference: measures this device's CUDA-core FMA throughput
+ * (QIW_PREC_FP64: DFMA, QIW_PREC_FP32: FFMA) in TFLOP/s with independent FMA chains on
+ * every SM, the roofline denominator of the evaluation kernels. */
+int qiw_measure_fma_peak(qiw_ctx *ctx, int32_t precision, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

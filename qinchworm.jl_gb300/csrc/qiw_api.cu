@@ -519,4 +519,33 @@ int qiw_integrate(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t
   return QIW_OK;
 }
 
+int qiw_measure_fma_peak(qiw_ctx *c, int32_t precision, double *tflops) {
+  if (!c || !tflops) return QIW_ERR_ARG;
+  cudaSetDevice(c->device);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  const int threads = 256, blocks = sms * 8, iters = 2048;
+  DevBuf<double> out;
+  int rc;
+  if ((rc = c->cuda(out.reserve((size_t)blocks * threads), "alloc"))) return rc;
+  const bool fp32 = precision == QIW_PREC_FP32;
+  double best = 0.0;
+  for (int rep = 0; rep < 4; ++rep) {
+    if ((rc = c->cuda(cudaEventRecord(c->ev0, c->stream), "event")) ||
+        (rc = c->cuda(launch_fma_peak(fp32, out.p, blocks, threads, iters, c->stream), "fma peak")) ||
+        (rc = c->cuda(cudaEventRecord(c->ev1, c->stream), "event")) ||
+        (rc = c->cuda(cudaEventSynchronize(c->ev1), "fma peak"))) {
+      out.release();
+      return rc;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    const double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+    if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+  }
+  out.release();
+  *tflops = best;
+  return QIW_OK;
+}
+
 }  // extern "C"

@@ -94,39 +94,60 @@ __device__ __forceinline__ void pmuld_u(T *A, int dst, int pm, int src) {
     for (int r = 0; r < R; ++r) A[dst + j * R + r] = p[r] * x[j * R + r];
 }
 
-template <typename T, int R, int K, int C>
-__device__ __forceinline__ void omul_u(T *A, const T *O, int dst, int oa, int src, T coef, bool accf) {
-  T o[R * K], x[K * C], y[R * C];
+// dst (=|+=) coef * O * src.  MODE 0: no coefficient (coef == 1 exactly), MODE 1: the
+// coefficient scales the smaller of src (K x C) and the product (R x C).
+template <typename T, int R, int K, int C, int MODE>
+__device__ __forceinline__ void omul_m(T *A, const T *O, int dst, int oa, int src, T coef, bool accf) {
+  T o[R * K], x[K * C];
 #pragma unroll
   for (int i = 0; i < R * K; ++i) o[i] = __ldg(O + oa + i);
 #pragma unroll
   for (int i = 0; i < K * C; ++i) x[i] = A[src + i];
-  if (accf) {
+  constexpr bool scale_src = (MODE == 1) && (K < R);
+  if (scale_src) {
 #pragma unroll
-    for (int i = 0; i < R * C; ++i) y[i] = A[dst + i];
+    for (int i = 0; i < K * C; ++i) x[i] *= coef;
   }
 #pragma unroll
   for (int j = 0; j < C; ++j)
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      T acc = o[r] * x[j * K];
+      const int d = dst + j * R + r;
+      T acc;
+      if (accf && !(MODE == 1 && !scale_src)) {
+        // accumulate into the destination: the chain starts from its value (K FMAs)
+        acc = A[d];
 #pragma unroll
-      for (int k = 1; k < K; ++k) acc = fmaT<T>(o[k * R + r], x[j * K + k], acc);
-      A[dst + j * R + r] = accf ? fmaT<T>(coef, acc, y[j * R + r]) : coef * acc;
+        for (int k = 0; k < K; ++k) acc = fmaT<T>(o[k * R + r], x[j * K + k], acc);
+      } else {
+        acc = o[r] * x[j * K];
+#pragma unroll
+        for (int k = 1; k < K; ++k) acc = fmaT<T>(o[k * R + r], x[j * K + k], acc);
+        if (MODE == 1 && !scale_src) acc = accf ? fmaT<T>(coef, acc, A[d]) : coef * acc;
+      }
+      A[d] = acc;
     }
 }
 
+template <typename T, int R, int K, int C>
+__device__ __forceinline__ void omul_u(T *A, const T *O, int dst, int oa, int src, T coef, bool accf,
+                                       bool has_coef) {
+  if (has_coef) omul_m<T, R, K, C, 1>(A, O, dst, oa, src, coef, accf);
+  else omul_m<T, R, K, C, 0>(A, O, dst, oa, src, coef, accf);
+}
+
 template <typename T, int N>
-__device__ __forceinline__ void axpy_u(T *A, int dst, int src, T coef, bool accf) {
-  T x[N], y[N];
+__device__ __forceinline__ void axpy_u(T *A, int dst, int src, T coef, bool accf, bool has_coef) {
+  T x[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) x[i] = A[src + i];
-  if (accf) {
+  if (has_coef) {
 #pragma unroll
-    for (int i = 0; i < N; ++i) y[i] = A[dst + i];
+    for (int i = 0; i < N; ++i) A[dst + i] = accf ? fmaT<T>(coef, x[i], A[dst + i]) : coef * x[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) A[dst + i] = accf ? x[i] + A[dst + i] : x[i];
   }
-#pragma unroll
-  for (int i = 0; i < N; ++i) A[dst + i] = accf ? fmaT<T>(coef, x[i], y[i]) : coef * x[i];
 }
 
 #define QIW_D3(F, ...)                                                                            \
@@ -212,11 +233,12 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
     }
     case OP_OMUL: {
       const int inner = I.inner;
-      const T coef = (I.w >= 0) ? (T)I.c * A[I.w] : (T)I.c;
+      const bool has_coef = (I.w >= 0) || (I.c != 1.0);
+      const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
       const int cr = dcode(rows), ck = dcode(inner), cc = dcode(cols);
       if (cr >= 0 && ck >= 0 && cc >= 0) {
         const int code = cr * 9 + ck * 3 + cc;
-        QIW_D3(omul_u, A, O, I.dst, I.a, I.src, coef, I.acc != 0)
+        QIW_D3(omul_u, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef)
       } else {
 #pragma unroll 1
         for (int j = 0; j < cols; ++j)
@@ -232,15 +254,16 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
       break;
     }
     case OP_AXPY: {
-      const T coef = (I.w >= 0) ? (T)I.c * A[I.w] : (T)I.c;
+      const bool has_coef = (I.w >= 0) || (I.c != 1.0);
+      const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
       const int n = rows * cols;
       const bool accf = I.acc != 0;
       switch (n) {
-        case 1: axpy_u<T, 1>(A, I.dst, I.src, coef, accf); break;
-        case 2: axpy_u<T, 2>(A, I.dst, I.src, coef, accf); break;
-        case 4: axpy_u<T, 4>(A, I.dst, I.src, coef, accf); break;
-        case 8: axpy_u<T, 8>(A, I.dst, I.src, coef, accf); break;
-        case 16: axpy_u<T, 16>(A, I.dst, I.src, coef, accf); break;
+        case 1: axpy_u<T, 1>(A, I.dst, I.src, coef, accf, has_coef); break;
+        case 2: axpy_u<T, 2>(A, I.dst, I.src, coef, accf, has_coef); break;
+        case 4: axpy_u<T, 4>(A, I.dst, I.src, coef, accf, has_coef); break;
+        case 8: axpy_u<T, 8>(A, I.dst, I.src, coef, accf, has_coef); break;
+        case 16: axpy_u<T, 16>(A, I.dst, I.src, coef, accf, has_coef); break;
         default:
 #pragma unroll 1
           for (int e = 0; e < n; ++e) {
@@ -261,7 +284,7 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
 }
 
 template <typename T, int ARENA, int RESMAX>
-__global__ void __launch_bounds__(kMaxThreads)
+__global__ void __launch_bounds__(kMaxThreads, kMinBlocks)
     eval_kernel(DevProblem pb, const DevGroup *__restrict__ groups, const DevWork *__restrict__ works,
                 const int4 *__restrict__ cta_map, double *__restrict__ partials) {
   const int4 cm = cta_map[blockIdx.x];   // (work item, batch, first sample of the tile, -)
@@ -435,6 +458,28 @@ __global__ void finish_kernel(const DevWork *__restrict__ works, const int *__re
     out[2 * ((size_t)out_off[wi] + e)] = 0.0;
     out[2 * ((size_t)out_off[wi] + e) + 1] = v;
   }
+}
+
+// FMA-throughput probe: 8 independent chains per thread keep the pipe full.
+template <typename T>
+__global__ void fma_peak_kernel(T *out, T b, T c, int iters) {
+  T a0 = (T)threadIdx.x, a1 = a0 + (T)1, a2 = a0 + (T)2, a3 = a0 + (T)3;
+  T a4 = a0 + (T)4, a5 = a0 + (T)5, a6 = a0 + (T)6, a7 = a0 + (T)7;
+#pragma unroll 1
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      a0 = fmaT<T>(a0, b, c); a1 = fmaT<T>(a1, b, c); a2 = fmaT<T>(a2, b, c); a3 = fmaT<T>(a3, b, c);
+      a4 = fmaT<T>(a4, b, c); a5 = fmaT<T>(a5, b, c); a6 = fmaT<T>(a6, b, c); a7 = fmaT<T>(a7, b, c);
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+cudaError_t launch_fma_peak(bool fp32, void *out, int blocks, int threads, int iters, cudaStream_t st) {
+  if (fp32) fma_peak_kernel<float><<<blocks, threads, 0, st>>>((float *)out, 0.999999f, 1e-7f, iters);
+  else fma_peak_kernel<double><<<blocks, threads, 0, st>>>((double *)out, 0.999999999, 1e-12, iters);
+  return cudaGetLastError();
 }
 
 template <typename T, int ARENA, int RESMAX>

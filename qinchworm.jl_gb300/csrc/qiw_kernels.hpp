@@ -9,6 +9,10 @@
 namespace qiw {
 
 constexpr int kMaxThreads = 128;     // samples per CTA (upper bound)
+#ifndef QIW_MIN_BLOCKS
+#define QIW_MIN_BLOCKS 4
+#endif
+constexpr int kMinBlocks = QIW_MIN_BLOCKS;  // 128-thread blocks per SM the register budget allows
 constexpr int kArenaSmall = 1024;    // per-sample arena instantiations (elements)
 constexpr int kArenaLarge = 8192;
 constexpr int kResSmall = 64;        // result-size instantiations (sum of d_s^2)
@@ -42,5 +46,6 @@ struct FinishArgs {
 int arena_class(int64_t arena);   // 0 small, 1 large, -1 too large
 cudaError_t launch_eval(const LaunchArgs &a);
 cudaError_t launch_finish(const FinishArgs &a);
+cudaError_t launch_fma_peak(bool fp32, void *out, int blocks, int threads, int iters, cudaStream_t st);
 
 }  // namespace qiw

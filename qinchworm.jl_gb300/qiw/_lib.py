@@ -29,7 +29,8 @@ QIW_PREC_FP64 = 0
 QIW_PREC_FP32 = 1
 
 EXPORTS = ["qiw_ctx_create", "qiw_ctx_destroy", "qiw_last_error", "qiw_problem_set", "qiw_ppgf_set",
-           "qiw_group_create", "qiw_group_stats_get", "qiw_integrate", "qiw_last_kernel_ms"]
+           "qiw_group_create", "qiw_group_stats_get", "qiw_integrate", "qiw_last_kernel_ms",
+           "qiw_measure_fma_peak"]
 
 
 class ProblemDesc(C.Structure):
@@ -81,6 +82,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
     lib.qiw_integrate.argtypes = [C.c_void_p, C.c_int32, C.POINTER(WorkDesc), C.c_int32, C.c_void_p]
     lib.qiw_last_kernel_ms.argtypes = [C.c_void_p]
     lib.qiw_last_kernel_ms.restype = C.c_double
+    lib.qiw_measure_fma_peak.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
     _lib = lib
     return lib
 

@@ -114,6 +114,11 @@ class Device:
             res.append(blocks)
         return res
 
+    def fma_peak_tflops(self, precision: int = _lib.QIW_PREC_FP64) -> float:
+        v = C.c_double()
+        self._check(self.lib.qiw_measure_fma_peak(self.h, precision, C.byref(v)))
+        return v.value
+
     def last_kernel_ms(self) -> float:
         return float(self.lib.qiw_last_kernel_ms(self.h))
 
