@@ -9,47 +9,11 @@
 #include <string>
 #include <vector>
 
-#include "qiw.h"
-#include "qiw_internal.hpp"
-#include "qiw_kernels.hpp"
-#include "qiw_plan.hpp"
+#include "qiw_ctx.hpp"
 
 using namespace qiw;
 
 namespace {
-
-template <typename T>
-struct DevBuf {
-  T *p = nullptr;
-  size_t n = 0;
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  cudaError_t reserve(size_t count) {
-    if (count <= n && p) return cudaSuccess;
-    release();
-    size_t c = std::max<size_t>(count, 1);
-    cudaError_t e = cudaMalloc(&p, c * sizeof(T));
-    if (e == cudaSuccess) n = c;
-    return e;
-  }
-  cudaError_t upload(const T *h, size_t count, cudaStream_t s) {
-    cudaError_t e = reserve(count);
-    if (e != cudaSuccess || count == 0) return e;
-    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
-  }
-};
-
-struct GroupRec {
-  Plan plan;
-  DevBuf<PmJob> pm;
-  DevBuf<WJob> wj;
-  DevBuf<Instr> ins;
-  DevBuf<int32_t> batch;
-  DevGroup dg;
-};
 
 // Natural cubic spline of y on a uniform grid; per segment a0 + a1 f + a2 f^2 + a3 f^3.
 void cubic_coeffs(const std::vector<double> &y, double h, std::vector<double> *out) {
@@ -85,79 +49,122 @@ double simplex_volume(int d, double edge) {
 
 }  // namespace
 
-struct qiw_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  std::string err;
-  double last_ms = 0.0;
+namespace qiw {
 
-  bool has_problem = false, has_P = false;
-  bool real_phase_problem = true, real_phase_P = true;
-  HostProblem hp;
-  int n_tau = 0;
-  double beta = 0.0, h = 0.0;
-  std::vector<int> dims, eoff, ptab_off, res_off, delta_kind, delta_off;
-  int64_t ptab_size = 0;
-  int res_total = 0;
-
-  DevBuf<int> d_dims, d_ptab_off, d_eoff, d_res_off, d_delta_kind, d_delta_off;
-  DevBuf<double> d_E, d_P, d_opv, d_delta;
-  DevBuf<float> d_Pf, d_opvf, d_deltaf;
-
-  std::vector<GroupRec *> groups;
-  DevBuf<DevGroup> d_groups;
-  bool groups_dirty = true;
-
-  DevBuf<DevWork> d_works;
-  DevBuf<int4> d_cta_map;
-  DevBuf<double> d_partials, d_out;
-  DevBuf<int> d_cta_first, d_res_sizes, d_out_off, d_err;
-  DevBuf<uint32_t> d_sobol;
-  int threads = 64;
-
-  int fail(int code, const std::string &msg) {
-    err = msg;
-    return code;
-  }
-  int cuda(cudaError_t e, const char *what) {
-    if (e == cudaSuccess) return QIW_OK;
-    err = std::string(what) + ": " + cudaGetErrorString(e);
-    return QIW_ERR_CUDA;
-  }
-  void clear_groups() {
-    for (auto *g : groups) {
-      g->pm.release();
-      g->wj.release();
-      g->ins.release();
-      g->batch.release();
-      delete g;
+int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, LaunchTables *t) {
+  if (precision != QIW_PREC_FP64 && precision != QIW_PREC_FP32)
+    return c->fail(QIW_ERR_ARG, "qiw_integrate: unknown precision");
+  if (!c->has_problem) return c->fail(QIW_ERR_ARG, "qiw_integrate: no problem set");
+  bool need_P = false;
+  t->works.assign(n_work, DevWork());
+  t->cta_first.assign(n_work, 0);
+  t->res_sizes.assign(n_work, 0);
+  t->out_off.assign(n_work, 0);
+  const int threads = c->threads;
+  for (int i = 0; i < n_work; ++i) {
+    const qiw_work_desc &wd = work[i];
+    if (wd.group < 0 || wd.group >= (int)c->groups.size()) return c->fail(QIW_ERR_ARG, "qiw_integrate: bad group id");
+    const Plan &p = c->groups[wd.group]->plan;
+    if (p.use_bold) need_P = true;
+    if (p.D > 0 && (!wd.sobol_m || !wd.sobol_x0)) return c->fail(QIW_ERR_ARG, "qiw_integrate: Sobol tables missing");
+    if (!(wd.t_i <= wd.t_f) || (p.kind != QIW_GROUP_BARE && !(wd.t_i <= wd.t_w && wd.t_w <= wd.t_f)))
+      return c->fail(QIW_ERR_ARG, "qiw_integrate: times must satisfy t_i <= t_w <= t_f");
+    if (p.D > 0 && (wd.n_total == 0 || wd.first_index + wd.n_samples > (1ull << 32)))
+      return c->fail(QIW_ERR_ARG, "qiw_integrate: Sobol index range beyond 2^32 or N_total = 0");
+    DevWork &w = t->works[i];
+    std::memset(&w, 0, sizeof(w));
+    w.group = wd.group;
+    w.t_i = wd.t_i;
+    w.t_w = wd.t_w;
+    w.t_f = wd.t_f;
+    w.first_index = wd.first_index;
+    if (p.D == 0) {
+      w.n_samples = 1;
+      w.scale = 1.0;  // order 0: evaluated exactly, no qMC average
+    } else {
+      w.n_samples = wd.n_samples;
+      double J = (p.kind == QIW_GROUP_BARE)
+                     ? simplex_volume(p.D, wd.t_f - wd.t_i)
+                     : simplex_volume(p.d_before, wd.t_w - wd.t_i) * simplex_volume(p.d_after, wd.t_f - wd.t_w);
+      w.scale = J / (double)wd.n_total;
     }
-    groups.clear();
-    groups_dirty = true;
+    const int n_tiles = (int)((w.n_samples + threads - 1) / threads);
+    const int n_b = std::max(0, (int)p.batch_begin.size() - 1);
+    w.n_cta = n_tiles * n_b;
+    t->cta_first[i] = (int)t->cta_map.size();
+    // heaviest batches first within the work item: the block scheduler then starts the
+    // long CTAs early (the finish kernel sums the partials in this same fixed order)
+    std::vector<int> order(n_b);
+    for (int b = 0; b < n_b; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return p.batch_flops[x] > p.batch_flops[y]; });
+    for (int b : order)
+      for (int k = 0; k < n_tiles; ++k) t->cta_map.push_back(make_int4(i, b, k * threads, 0));
+    t->res_sizes[i] = p.res_size;
+    t->out_off[i] = t->out_total;
+    t->out_total += p.res_size;
+    t->arena_max = std::max<int64_t>(t->arena_max, p.arena);
+    t->res_max = std::max(t->res_max, p.res_size);
+    // Sobol tables: offsets into t->sobol, turned into device pointers when placed
+    w.m = reinterpret_cast<const uint32_t *>((uintptr_t)t->sobol.size());
+    if (p.D > 0) t->sobol.insert(t->sobol.end(), wd.sobol_m, wd.sobol_m + 32 * p.D);
+    w.x0 = reinterpret_cast<const uint32_t *>((uintptr_t)t->sobol.size());
+    if (p.D > 0) t->sobol.insert(t->sobol.end(), wd.sobol_x0, wd.sobol_x0 + p.D);
   }
-  DevProblem dev_problem(bool fp32) const {
-    DevProblem p;
-    std::memset(&p, 0, sizeof(p));
-    p.S = hp.S;
-    p.n_tau = n_tau;
-    p.n_pairs = hp.n_pairs;
-    p.h = h;
-    p.inv_h = 1.0 / h;
-    p.beta = beta;
-    p.dims = d_dims.p;
-    p.ptab_off = d_ptab_off.p;
-    p.eoff = d_eoff.p;
-    p.res_off = d_res_off.p;
-    p.E = d_E.p;
-    p.P = fp32 ? (const void *)d_Pf.p : (const void *)d_P.p;
-    p.opv = fp32 ? (const void *)d_opvf.p : (const void *)d_opv.p;
-    p.delta = fp32 ? (const void *)d_deltaf.p : (const void *)d_delta.p;
-    p.delta_kind = d_delta_kind.p;
-    p.delta_off = d_delta_off.p;
-    return p;
-  }
-};
+  if (!c->real_phase_problem || (need_P && !c->real_phase_P))
+    return c->fail(QIW_ERR_UNSUPPORTED, "qiw_integrate: inputs are not real-phase (i*P, i*Delta and operator "
+                                        "blocks must be real); only the real-phase kernels are built");
+  if (need_P && !c->has_P) return c->fail(QIW_ERR_ARG, "qiw_integrate: bold group but qiw_ppgf_set was not called");
+  if (t->res_max > kResLarge) return c->fail(QIW_ERR_UNSUPPORTED, "qiw_integrate: sum of d_s^2 above 512");
+  return QIW_OK;
+}
+
+int sync_groups(qiw_ctx *c) {
+  if (!c->groups_dirty) return QIW_OK;
+  std::vector<DevGroup> dgs;
+  for (auto *g : c->groups) dgs.push_back(g->dg);
+  int rc = c->cuda(c->d_groups.upload(dgs.data(), dgs.size(), c->stream), "upload groups");
+  if (rc) return rc;
+  c->groups_dirty = false;
+  return QIW_OK;
+}
+
+// Launches the evaluation and finish kernels on tables already placed in device memory.
+int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const DevGroup *groups, const DevWork *works,
+                  const int4 *cta_map, const int *cta_first, const int *res_sizes, const int *out_off,
+                  double *partials, int *err, double *out) {
+  const int n_cta = (int)t.cta_map.size();
+  LaunchArgs la;
+  la.pb = c->dev_problem(precision == QIW_PREC_FP32);
+  la.groups = groups;
+  la.works = works;
+  la.cta_map = cta_map;
+  la.partials = partials;
+  la.n_cta = n_cta;
+  la.threads = c->threads;
+  la.arena_max = t.arena_max;
+  la.res_max = t.res_max;
+  la.fp32 = precision == QIW_PREC_FP32;
+  la.stream = c->stream;
+  FinishArgs fa;
+  fa.works = works;
+  fa.cta_first = cta_first;
+  fa.partials = partials;
+  fa.res_sizes = res_sizes;
+  fa.out_off = out_off;
+  fa.out = out;
+  fa.err_word = err;
+  fa.n_work = (int)t.works.size();
+  fa.stream = c->stream;
+  int rc;
+  if ((rc = c->cuda(cudaEventRecord(c->ev0, c->stream), "event")) ||
+      (n_cta > 0 && (rc = c->cuda(launch_eval(la), "eval kernel launch"))) ||
+      (rc = c->cuda(launch_finish(fa), "finish kernel launch")) || (rc = c->cuda(cudaEventRecord(c->ev1, c->stream), "event")))
+    return rc;
+  return QIW_OK;
+}
+
+}  // namespace qiw
 
 extern "C" {
 
@@ -390,125 +397,34 @@ int qiw_group_stats_get(qiw_ctx *c, int32_t gid, qiw_group_stats *out) {
 
 int qiw_integrate(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, double *out) {
   if (!c || n_work < 0 || (n_work > 0 && (!work || !out))) return QIW_ERR_ARG;
-  if (precision != QIW_PREC_FP64 && precision != QIW_PREC_FP32) return c->fail(QIW_ERR_ARG, "qiw_integrate: unknown precision");
-  if (!c->has_problem) return c->fail(QIW_ERR_ARG, "qiw_integrate: no problem set");
   cudaSetDevice(c->device);
   if (n_work == 0) return QIW_OK;
-  bool need_P = false;
-  std::vector<DevWork> works(n_work);
-  std::vector<int4> cta_map;
-  std::vector<int> cta_first(n_work), res_sizes(n_work), out_off(n_work);
-  std::vector<uint32_t> sob;
-  int64_t arena_max = 0;
-  int res_max = 0, out_total = 0;
-  const int threads = c->threads;
-  for (int i = 0; i < n_work; ++i) {
-    const qiw_work_desc &wd = work[i];
-    if (wd.group < 0 || wd.group >= (int)c->groups.size()) return c->fail(QIW_ERR_ARG, "qiw_integrate: bad group id");
-    const Plan &p = c->groups[wd.group]->plan;
-    if (p.use_bold) need_P = true;
-    if (p.D > 0 && (!wd.sobol_m || !wd.sobol_x0)) return c->fail(QIW_ERR_ARG, "qiw_integrate: Sobol tables missing");
-    if (!(wd.t_i <= wd.t_f) || (p.kind != QIW_GROUP_BARE && !(wd.t_i <= wd.t_w && wd.t_w <= wd.t_f)))
-      return c->fail(QIW_ERR_ARG, "qiw_integrate: times must satisfy t_i <= t_w <= t_f");
-    if (p.D > 0 && (wd.n_total == 0 || wd.first_index + wd.n_samples > (1ull << 32)))
-      return c->fail(QIW_ERR_ARG, "qiw_integrate: Sobol index range beyond 2^32 or N_total = 0");
-    DevWork &w = works[i];
-    std::memset(&w, 0, sizeof(w));
-    w.group = wd.group;
-    w.t_i = wd.t_i;
-    w.t_w = wd.t_w;
-    w.t_f = wd.t_f;
-    w.first_index = wd.first_index;
-    if (p.D == 0) {
-      w.n_samples = 1;
-      w.scale = 1.0;  // order 0: evaluated exactly, no qMC average
-    } else {
-      w.n_samples = wd.n_samples;
-      double J = (p.kind == QIW_GROUP_BARE)
-                     ? simplex_volume(p.D, wd.t_f - wd.t_i)
-                     : simplex_volume(p.d_before, wd.t_w - wd.t_i) * simplex_volume(p.d_after, wd.t_f - wd.t_w);
-      w.scale = J / (double)wd.n_total;
-    }
-    const int n_tiles = (int)((w.n_samples + threads - 1) / threads);
-    const int n_b = std::max(0, (int)p.batch_begin.size() - 1);
-    w.n_cta = n_tiles * n_b;
-    cta_first[i] = (int)cta_map.size();
-    // heaviest batches first within the work item: the block scheduler then starts the
-    // long CTAs early (the finish kernel sums the partials in this same fixed order)
-    std::vector<int> order(n_b);
-    for (int b = 0; b < n_b; ++b) order[b] = b;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int x, int y) { return p.batch_flops[x] > p.batch_flops[y]; });
-    for (int b : order)
-      for (int k = 0; k < n_tiles; ++k) cta_map.push_back(make_int4(i, b, k * threads, 0));
-    res_sizes[i] = p.res_size;
-    out_off[i] = out_total;
-    out_total += p.res_size;
-    arena_max = std::max<int64_t>(arena_max, p.arena);
-    res_max = std::max(res_max, p.res_size);
-    // Sobol tables: stash host offsets in the pointer fields, patched after upload
-    w.m = reinterpret_cast<const uint32_t *>((uintptr_t)sob.size());
-    if (p.D > 0) sob.insert(sob.end(), wd.sobol_m, wd.sobol_m + 32 * p.D);
-    w.x0 = reinterpret_cast<const uint32_t *>((uintptr_t)sob.size());
-    if (p.D > 0) sob.insert(sob.end(), wd.sobol_x0, wd.sobol_x0 + p.D);
-  }
-  if (!c->real_phase_problem || (need_P && !c->real_phase_P))
-    return c->fail(QIW_ERR_UNSUPPORTED, "qiw_integrate: inputs are not real-phase (i*P, i*Delta and operator "
-                                        "blocks must be real); only the real-phase kernels are built");
-  if (need_P && !c->has_P) return c->fail(QIW_ERR_ARG, "qiw_integrate: bold group but qiw_ppgf_set was not called");
-  if (res_max > kResLarge) return c->fail(QIW_ERR_UNSUPPORTED, "qiw_integrate: sum of d_s^2 above 512");
-  int rc;
+  LaunchTables t;
+  int rc = prepare_launch(c, n_work, work, precision, &t);
+  if (rc) return rc;
+  if ((rc = sync_groups(c))) return rc;
   cudaStream_t st = c->stream;
-  if ((rc = c->cuda(c->d_sobol.upload(sob.data(), sob.size(), st), "upload Sobol"))) return rc;
-  for (auto &w : works) {
+  if ((rc = c->cuda(c->d_sobol.upload(t.sobol.data(), t.sobol.size(), st), "upload Sobol"))) return rc;
+  for (auto &w : t.works) {
     w.m = c->d_sobol.p + (uintptr_t)w.m;
     w.x0 = c->d_sobol.p + (uintptr_t)w.x0;
   }
-  if (c->groups_dirty) {
-    std::vector<DevGroup> dgs;
-    for (auto *g : c->groups) dgs.push_back(g->dg);
-    if ((rc = c->cuda(c->d_groups.upload(dgs.data(), dgs.size(), st), "upload groups"))) return rc;
-    c->groups_dirty = false;
-  }
-  const int n_cta = (int)cta_map.size();
+  const int n_cta = (int)t.cta_map.size();
   int zero = 0;
-  if ((rc = c->cuda(c->d_works.upload(works.data(), works.size(), st), "upload work")) ||
-      (rc = c->cuda(c->d_cta_map.upload(cta_map.data(), cta_map.size(), st), "upload work")) ||
-      (rc = c->cuda(c->d_cta_first.upload(cta_first.data(), cta_first.size(), st), "upload work")) ||
-      (rc = c->cuda(c->d_res_sizes.upload(res_sizes.data(), res_sizes.size(), st), "upload work")) ||
-      (rc = c->cuda(c->d_out_off.upload(out_off.data(), out_off.size(), st), "upload work")) ||
+  if ((rc = c->cuda(c->d_works.upload(t.works.data(), t.works.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_cta_map.upload(t.cta_map.data(), t.cta_map.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_cta_first.upload(t.cta_first.data(), t.cta_first.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_res_sizes.upload(t.res_sizes.data(), t.res_sizes.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_out_off.upload(t.out_off.data(), t.out_off.size(), st), "upload work")) ||
       (rc = c->cuda(c->d_err.upload(&zero, 1, st), "upload work")) ||
-      (rc = c->cuda(c->d_partials.reserve((size_t)n_cta * res_max), "alloc partials")) ||
-      (rc = c->cuda(c->d_out.reserve((size_t)2 * out_total), "alloc out")))
+      (rc = c->cuda(c->d_partials.reserve((size_t)n_cta * t.res_max), "alloc partials")) ||
+      (rc = c->cuda(c->d_out.reserve((size_t)2 * t.out_total), "alloc out")))
     return rc;
-  LaunchArgs la;
-  la.pb = c->dev_problem(precision == QIW_PREC_FP32);
-  la.groups = c->d_groups.p;
-  la.works = c->d_works.p;
-  la.cta_map = c->d_cta_map.p;
-  la.partials = c->d_partials.p;
-  la.n_cta = n_cta;
-  la.threads = threads;
-  la.arena_max = arena_max;
-  la.res_max = res_max;
-  la.fp32 = precision == QIW_PREC_FP32;
-  la.stream = st;
-  FinishArgs fa;
-  fa.works = c->d_works.p;
-  fa.cta_first = c->d_cta_first.p;
-  fa.partials = c->d_partials.p;
-  fa.res_sizes = c->d_res_sizes.p;
-  fa.out_off = c->d_out_off.p;
-  fa.out = c->d_out.p;
-  fa.err_word = c->d_err.p;
-  fa.n_work = n_work;
-  fa.stream = st;
-  if ((rc = c->cuda(cudaEventRecord(c->ev0, st), "event")) ||
-      (n_cta > 0 && (rc = c->cuda(launch_eval(la), "eval kernel launch"))) ||
-      (rc = c->cuda(launch_finish(fa), "finish kernel launch")) || (rc = c->cuda(cudaEventRecord(c->ev1, st), "event")))
-    return rc;
+  rc = launch_tables(c, t, precision, c->d_groups.p, c->d_works.p, c->d_cta_map.p, c->d_cta_first.p, c->d_res_sizes.p,
+                     c->d_out_off.p, c->d_partials.p, c->d_err.p, c->d_out.p);
+  if (rc) return rc;
   int err_word = 0;
-  if ((rc = c->cuda(cudaMemcpyAsync(out, c->d_out.p, sizeof(double) * 2 * out_total, cudaMemcpyDeviceToHost, st), "copy out")) ||
+  if ((rc = c->cuda(cudaMemcpyAsync(out, c->d_out.p, sizeof(double) * 2 * t.out_total, cudaMemcpyDeviceToHost, st), "copy out")) ||
       (rc = c->cuda(cudaMemcpyAsync(&err_word, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "copy err")) ||
       (rc = c->cuda(cudaStreamSynchronize(st), "integrate")))
     return rc;
