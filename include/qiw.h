@@ -137,6 +137,16 @@ typedef struct {
 int qiw_integrate(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, int32_t precision,
                   double *out);
 
+/* No counterpart in the reference.  qiw_integrate for callers that cannot allocate device
+ * memory while they run: it allocates nothing.  Its scratch (launch tables, Sobol tables,
+ * per-CTA partial sums) is one 16 MiB static device array per GPU, held until the process
+ * exits; calls that need more are rejected with QIW_ERR_MEMORY.  `out_device` is a device
+ * buffer the caller owns, laid out like qiw_integrate's `out`.  The first call on a device
+ * looks the array's address up (make it before any stream capture).  All calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the caller. */
+int qiw_integrate_noalloc(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, int32_t precision,
+                          double *out_device);
+
 /* Kernel time of the most recent qiw_integrate (ms, CUDA events on the context stream). */
 double qiw_last_kernel_ms(const qiw_ctx *ctx);
 

@@ -30,7 +30,7 @@ QIW_PREC_FP32 = 1
 
 EXPORTS = ["qiw_ctx_create", "qiw_ctx_destroy", "qiw_last_error", "qiw_problem_set", "qiw_ppgf_set",
            "qiw_group_create", "qiw_group_stats_get", "qiw_integrate", "qiw_last_kernel_ms",
-           "qiw_measure_fma_peak"]
+           "qiw_measure_fma_peak", "qiw_integrate_noalloc"]
 
 
 class ProblemDesc(C.Structure):
@@ -83,6 +83,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
     lib.qiw_last_kernel_ms.argtypes = [C.c_void_p]
     lib.qiw_last_kernel_ms.restype = C.c_double
     lib.qiw_measure_fma_peak.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
+    lib.qiw_integrate_noalloc.argtypes = [C.c_void_p, C.c_int32, C.POINTER(WorkDesc), C.c_int32, C.c_void_p]
     _lib = lib
     return lib
 
