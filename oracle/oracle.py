@@ -79,6 +79,9 @@ def lib():
         _lib.qiwo_sobol_directions.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         _lib.qiwo_sobol_points.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p]
         _lib.qiwo_natural_spline_M.argtypes = [C.c_int, C.c_double, C.c_void_p, C.c_void_p]
+        _lib.qiwo_integrate_range.restype = C.c_int
+        _lib.qiwo_integrate_range.argtypes = [C.POINTER(_Problem), C.POINTER(_Group), C.c_void_p, C.c_void_p,
+                                              C.c_int64, C.c_int64, C.c_int64, C.c_void_p]
     return _lib
 
 
@@ -278,7 +281,8 @@ class OracleProblem:
         return pb, Ps
 
     def integrate(self, kind: str, order: int, n_pts_after: int, tops, t_i: float, t_w: float,
-                  t_f: float, N: int, n_ranks: int = 1, m=None, x0=None, corr: Optional[int] = None):
+                  t_f: float, N: int, n_ranks: int = 1, m=None, x0=None, corr: Optional[int] = None,
+                  sample_range=None):
         """One group: kind 'bold', 'bare' or 'corr'; returns per-sector diagonal blocks."""
         if kind == "bare":
             fixed = [(0, 2, 0, t_i), (2 * order + 1, 2, 0, t_f)]
@@ -308,7 +312,11 @@ class OracleProblem:
         x0 = np.zeros(max(D, 1), np.uint32) if x0 is None else np.ascontiguousarray(x0, dtype=np.uint32)
         out = np.zeros(int(np.sum(self.dims ** 2)), dtype=np.complex128)
         pb, _keep = self._problem()
-        rc = lib().qiwo_integrate(C.byref(pb), C.byref(gr), _ptr(m), _ptr(x0), N, n_ranks, _ptr(out))
+        if sample_range is None:
+            rc = lib().qiwo_integrate(C.byref(pb), C.byref(gr), _ptr(m), _ptr(x0), N, n_ranks, _ptr(out))
+        else:
+            first, count = sample_range
+            rc = lib().qiwo_integrate_range(C.byref(pb), C.byref(gr), _ptr(m), _ptr(x0), first, count, N, _ptr(out))
         if rc == 2:
             raise AssertionError("A block off-diagonal contribution to a pseudo-particle propagator detected")
         if rc:

@@ -592,3 +592,26 @@ int qiwo_integrate(const qiwo_problem *pb, const qiwo_group *gr, const uint32_t 
     free(bufs);
     return rc;
 }
+
+/* One rank's share: samples [first, first + count) of N_total, weighted count/N_total
+ * (rank_weight * contour_integral over the rank's range, src/inchworm.jl:168-187). */
+int qiwo_integrate_range(const qiwo_problem *pb, const qiwo_group *gr, const uint32_t *m, const uint32_t *x0,
+                         int64_t first, int64_t count, int64_t N_total, double *out)
+{
+    int S = pb->n_sectors;
+    cplx *buf = calloc((size_t)S * BLK, sizeof(cplx));
+    job_t jb = (job_t){pb, gr, m, x0, first, gr->order == 0 ? 1 : count, gr->order == 0 ? 1 : N_total, buf, 0};
+    if (jb.count > 0) run_range(&jb);
+    size_t off = 0;
+    for (int s = 0; s < S; ++s) {
+        int d = pb->dims[s];
+        for (int e = 0; e < d * d; ++e) {
+            cplx v = jb.count > 0 ? buf[(size_t)s * BLK + e] : 0;
+            out[2 * (off + e)] = creal(v);
+            out[2 * (off + e) + 1] = cimag(v);
+        }
+        off += (size_t)d * d;
+    }
+    free(buf);
+    return jb.rc;
+}

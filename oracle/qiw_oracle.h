@@ -71,4 +71,7 @@ void qiwo_natural_spline_M(int n, double h, const double *y, double *M);
 int qiwo_integrate(const qiwo_problem *pb, const qiwo_group *gr, const uint32_t *m, const uint32_t *x0,
                    int64_t N, int n_ranks, double *out);
 
+int qiwo_integrate_range(const qiwo_problem *pb, const qiwo_group *gr, const uint32_t *m, const uint32_t *x0,
+                         int64_t first, int64_t count, int64_t N_total, double *out);
+
 #endif

@@ -1,0 +1,97 @@
+"""Sample-range decomposition over ranks (src/mpi.jl:49-54, 104-127) with a real
+torch.distributed all-reduce (gloo, world size 2, CPU).  The per-rank integrals come from the
+CPU oracle through a stand-in for the device, so the host-side rank logic of qiw.inchworm --
+rank_sub_range, Sobol index offsets, rank weights and the packed all-reduce -- is what is
+under test."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch.multiprocessing as mp
+
+
+class OracleDevice:
+    """Duck-typed stand-in for qiw.device.Device backed by the CPU oracle."""
+
+    def __init__(self):
+        self.groups = {}
+        self.group_info = {}
+
+    def set_problem(self, exp):
+        import oracle as orc
+        self.pb = orc.OracleProblem(exp)
+        self.exp = exp
+        self.groups.clear()
+        return None
+
+    def set_ppgf(self, P):
+        for s, P_s in enumerate(P):
+            self.pb.P_data[s] = np.ascontiguousarray(P_s.data.copy())
+
+    def create_group(self, kind, order, n_pts_after, tops, corr=None):
+        gid = len(self.groups)
+        okind = {0: "bold", 1: "bare", 2: "corr"}[kind]
+        self.groups[gid] = (okind, order, n_pts_after, [(t.pairs, t.parity) for t in tops], corr)
+        self.group_info[gid] = (kind, order, n_pts_after)
+        return gid
+
+    def integrate(self, works, precision=0):
+        out = []
+        for w in works:
+            okind, order, npa, tops, corr = self.groups[w.group]
+            out.append(self.pb.integrate(okind, order, npa, tops, w.t_i, w.t_w, w.t_f, w.n_total, corr=corr,
+                                         m=w.sobol_m, x0=w.sobol_x0, sample_range=(w.first_index, w.n_samples)))
+        return out
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, q):
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for p in (os.path.join(root, "qinchworm.jl_gb300"), os.path.join(root, "oracle"), os.path.join(root, "tests")):
+        sys.path.insert(0, p)
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from qiw import models
+    from qiw.inchworm import inchworm, TorchComm
+    from test_multirank import OracleDevice
+    exp = models.anderson(n_tau=8)
+    inchworm(exp, range(0, 3), range(0, 3), 32, dev=OracleDevice(), comm=TorchComm())
+    q.put((rank, [P_s.data.copy() for P_s in exp.P]))
+    dist.destroy_process_group()
+
+
+def test_two_rank_inchworm_equals_single_rank():
+    import oracle as orc
+    from qiw import models
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = {}
+    for _ in procs:
+        try:
+            r, P = q.get(timeout=900)
+        except Exception:
+            break
+        res[r] = P
+    for p in procs:
+        p.join(timeout=300)
+        assert p.exitcode == 0
+    assert sorted(res) == [0, 1]
+    exp = models.anderson(n_tau=8)
+    pb = orc.inchworm(exp, range(0, 3), range(0, 3), 32)   # one rank, 32 samples (ranks: 16 + 16)
+    for s in range(len(pb.P_data)):
+        want = pb.P_data[s]
+        for r in (0, 1):
+            got = res[r][s]
+            assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
