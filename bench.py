@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--model", default="eg", choices=["eg", "anderson"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy"])
+    ap.add_argument("--n-tau", type=int, default=32, help="accuracy mode: tau grid size")
+    ap.add_argument("--n-ref", type=int, default=2 ** 15, help="accuracy mode: samples of the FP64 reference")
+    ap.add_argument("--n-max", type=int, default=2 ** 13, help="accuracy mode: largest swept N")
     return ap.parse_args()
 
 
@@ -284,9 +288,69 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+def _solve(model, n_tau, N, prec, dev, corr=False):
+    """Full inchworm! on the GPU; returns (P normalised by beta as arrays, G or None, seconds)."""
+    import torch
+    from qiw import models, ppgf
+    from qiw.inchworm import inchworm, correlator_2p
+    exp = models.eg_discrete_bath(n_tau=n_tau, corr=corr) if model == "eg" else models.anderson(n_tau=n_tau, corr=corr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    inchworm(exp, range(0, 5), range(0, 5), N, dev=dev, precision=prec)
+    el = time.perf_counter() - t0
+    ppgf.normalize_beta(exp.P, exp.grid.beta)
+    G = None
+    if corr:
+        G = np.array(correlator_2p(exp, range(0, 4), N, dev=dev, precision=prec))
+    return [P_s.data.copy() for P_s in exp.P], G, el
+
+
+def _perr(P, Q):
+    return max(float(np.abs(a - b).max()) for a, b in zip(P, Q))
+
+
+def run_accuracy(args):
+    """Time to 1e-4 max |P(tau) - P_ref(tau)| for the plain FP64 and the FP32-chain paths
+    against a plain FP64 run at args.n_ref samples, plus max |P_FP32 - P_FP64| and the G(tau)
+    difference at equal N (same Sobol points)."""
+    from qiw import _lib
+    from qiw.device import Device
+    dev = Device(int(os.environ.get("LOCAL_RANK", "0")))
+    P_ref, _, t_ref = _solve(args.model, args.n_tau, args.n_ref, _lib.QIW_PREC_FP64, dev)
+    sweep = []
+    N = 256
+    while N <= args.n_max:
+        row = {"N": N}
+        P64, G64, t64 = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP64, dev, corr=(N == 1024))
+        P32, G32, t32 = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, corr=(N == 1024))
+        row.update(err_fp64=_perr(P64, P_ref), err_fp32=_perr(P32, P_ref), s_fp64=t64, s_fp32=t32,
+                   fp32_vs_fp64_P=_perr(P32, P64))
+        if G64 is not None:
+            row["fp32_vs_fp64_G"] = float(np.abs(G32 - G64).max())
+        sweep.append(row)
+        N *= 2
+
+    def ttt(key_err, key_t):
+        for r in sweep:
+            if r[key_err] <= 1e-4:
+                return r[key_t], r["N"]
+        return None, None
+
+    t64, n64 = ttt("err_fp64", "s_fp64")
+    t32, n32 = ttt("err_fp32", "s_fp32")
+    print(json.dumps({"mode": "accuracy", "metric": "time to 1e-4 max |P(tau) - P_ref(tau)|", "unit": "s",
+                      "config": {"model": args.model, "n_tau": args.n_tau, "orders": "0:4", "N_ref": args.n_ref,
+                                 "reference": "plain FP64 GPU run at N_ref (Sobol, same grid)"},
+                      "time_to_1e-4_fp64": t64, "N_fp64": n64, "time_to_1e-4_fp32": t32, "N_fp32": n32,
+                      "speedup_fp32": (t64 / t32) if (t64 and t32) else None,
+                      "reference_solve_s": t_ref, "sweep": sweep}))
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.mode == "accuracy":
+        run_accuracy(a)
     else:
         run_ours(a)

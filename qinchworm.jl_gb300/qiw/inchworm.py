@@ -127,10 +127,10 @@ class _Session:
             n_seqs = 1 if td.order == 0 else td.rand_params.N_seqs
             for s in range(n_seqs):
                 if D == 0 or td.rand_params.rng is None:
-                    m = direction_numbers(D) if D else None
+                    m = self.dev.sobol(D) if D else None
                     x0 = np.zeros(D, np.uint32) if D else None
                 else:
-                    m, x0 = scramble(direction_numbers(D), td.rand_params.rng)
+                    m, x0 = scramble(self.dev.sobol(D), td.rand_params.rng)
                 seqs.append((m, x0))
             plan.append((gid, td, seqs))
         # one launch for every (group, sequence) of the step
@@ -321,9 +321,9 @@ def _run_multi_tau(ses: _Session, all_tds, spans, times, precision, comm, corr):
             n_seqs = 1 if td.order == 0 else td.rand_params.N_seqs
             for s in range(n_seqs):
                 if D == 0 or td.rand_params.rng is None:
-                    m, x0 = (direction_numbers(D), np.zeros(D, np.uint32)) if D else (None, None)
+                    m, x0 = (ses.dev.sobol(D), np.zeros(D, np.uint32)) if D else (None, None)
                 else:
-                    m, x0 = scramble(direction_numbers(D), td.rand_params.rng)
+                    m, x0 = scramble(ses.dev.sobol(D), td.rand_params.rng)
                 start, length = rank_sub_range(td.N_samples, comm) if td.order > 0 else (0, 1)
                 works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
                 index.append((q, a + k))

@@ -177,3 +177,21 @@ def test_correlator_matches_oracle(device):
     want = orc.correlator_2p(pb, range(0, 3), 64)
     for a, b in zip(got, want):
         assert np.abs(a - b).max() <= 1e-11 * np.abs(b).max()
+
+
+def test_fp32_path_errors_are_stated_and_small(device):
+    """FP32 chain products with FP64 accumulation: max |P_FP32 - P_FP64| and the G(tau)
+    difference on a full inchworm! + correlator_2p run with the same Sobol points."""
+    from qiw import ppgf
+    from qiw.inchworm import inchworm, correlator_2p
+    res = {}
+    for prec in (_lib.QIW_PREC_FP64, _lib.QIW_PREC_FP32):
+        exp = models.anderson(n_tau=24, corr=True)
+        inchworm(exp, range(0, 4), range(0, 4), 256, dev=device, precision=prec)
+        ppgf.normalize_beta(exp.P, exp.grid.beta)
+        g = correlator_2p(exp, range(0, 3), 256, dev=device, precision=prec)
+        res[prec] = ([P_s.data.copy() for P_s in exp.P], np.array(g))
+    dP = max(np.abs(a - b).max() for a, b in zip(res[0][0], res[1][0]))
+    dG = np.abs(res[0][1] - res[1][1]).max()
+    print(f"FP32 vs FP64: max|dP| = {dP:.2e}, max|dG| = {dG:.2e}")
+    assert dP < 1e-5 and dG < 1e-5
