@@ -29,6 +29,10 @@ class OracleDevice:
         for s, P_s in enumerate(P):
             self.pb.P_data[s] = np.ascontiguousarray(P_s.data.copy())
 
+    def sobol(self, D):
+        from qiw.sobol import direction_numbers
+        return direction_numbers(D)
+
     def create_group(self, kind, order, n_pts_after, tops, corr=None):
         gid = len(self.groups)
         okind = {0: "bold", 1: "bare", 2: "corr"}[kind]
@@ -77,13 +81,17 @@ def test_two_rank_inchworm_equals_single_rank():
     procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
+    import queue
+    import time
     res = {}
-    for _ in procs:
+    deadline = time.time() + 900
+    while len(res) < len(procs) and time.time() < deadline:
         try:
-            r, P = q.get(timeout=900)
-        except Exception:
-            break
-        res[r] = P
+            r, P = q.get(timeout=5)
+            res[r] = P
+        except queue.Empty:
+            if any(p.exitcode not in (None, 0) for p in procs):
+                break
     for p in procs:
         p.join(timeout=300)
         assert p.exitcode == 0
