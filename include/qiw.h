@@ -147,6 +147,37 @@ int qiw_integrate(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, int32
 int qiw_integrate_noalloc(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, int32_t precision,
                           double *out_device);
 
+/*
+ * Learned change of variables (no counterpart in the reference; its closest relative is the
+ * hand-made ExpModelFunctionTransform, src/qmc_integrate.jl:99-165).  A warp is a triangular
+ * monotone map x = w(y) of [0,1]^D (D = 2*order <= 8): per dimension a 16-bin piecewise-linear
+ * CDF whose bin masses come from a masked MLP (3 hidden layers of 64, BF16 weights, FP32
+ * accumulation).  qiw_integrate_warped evaluates f(u(w(y))) J / q(w(y)) on the Sobol points
+ * y: unbiased for any weights, so plain qMC stays the reference for its variance and error.
+ */
+int qiw_warp_create(qiw_ctx *ctx, int32_t D, uint64_t seed, int32_t *warp_id);
+/* Weight a in (0, 1] of the uniform density in q (default 0.3): 1/q <= a^-D. */
+int qiw_warp_set_mix(qiw_ctx *ctx, int32_t warp_id, double uniform_mix);
+int qiw_warp_n_params(qiw_ctx *ctx, int32_t warp_id, int64_t *n);
+int qiw_warp_get_params(qiw_ctx *ctx, int32_t warp_id, double *params);
+int qiw_warp_set_params(qiw_ctx *ctx, int32_t warp_id, const double *params);
+/* Gradient of the |f|-weighted negative log-likelihood -sum_i w_i log q(x_i) / sum_i w_i. */
+int qiw_warp_grad(qiw_ctx *ctx, int32_t warp_id, const double *x, const double *w, int64_t n, double *grad,
+                  double *loss);
+/* Adam on minibatches of (x_i in [0,1)^D, w_i = |f(x_i)|) produced by plain qMC. */
+int qiw_warp_train(qiw_ctx *ctx, int32_t warp_id, const double *x, const double *w, int64_t n, int32_t steps,
+                   int32_t batch, double lr, double *final_loss);
+/* Warped points of Sobol indices first..first+n-1: [n][D + 1] = (x_1..x_D, 1/q(x)). */
+int qiw_warp_map(qiw_ctx *ctx, int32_t warp_id, const uint32_t *sobol_m, const uint32_t *sobol_x0,
+                 uint64_t first, uint64_t n, double *points);
+/* qiw_integrate with a warp per work item (warp_ids[i] = -1: plain qMC). */
+int qiw_integrate_warped(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, const int32_t *warp_ids,
+                         int32_t precision, double *out);
+/* qiw_integrate of one work item that also returns the per-sample integrand values
+ * samples[n_samples][sum d_s^2] (real parts f_i with out = -i * J / N * sum_i f_i). */
+int qiw_integrate_samples(qiw_ctx *ctx, const qiw_work_desc *work, int32_t precision, double *out,
+                          double *samples);
+
 /* Kernel time of the most recent qiw_integrate (ms, CUDA events on the context stream). */
 double qiw_last_kernel_ms(const qiw_ctx *ctx);
 

@@ -51,6 +51,84 @@ double simplex_volume(int d, double edge) {
 
 namespace qiw {
 
+int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, double *out,
+                   const int32_t *warp_ids, double *sample_out) {
+  if (!c || n_work < 0 || (n_work > 0 && (!work || !out))) return QIW_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (n_work == 0) return QIW_OK;
+  LaunchTables t;
+  int rc = prepare_launch(c, n_work, work, precision, &t);
+  if (rc) return rc;
+  if ((rc = sync_groups(c))) return rc;
+  cudaStream_t st = c->stream;
+  if ((rc = c->cuda(c->d_sobol.upload(t.sobol.data(), t.sobol.size(), st), "upload Sobol"))) return rc;
+  for (auto &w : t.works) {
+    w.m = c->d_sobol.p + (uintptr_t)w.m;
+    w.x0 = c->d_sobol.p + (uintptr_t)w.x0;
+  }
+  // warped points: one buffer, one region per warped work item
+  if (warp_ids) {
+    size_t total = 0;
+    std::vector<size_t> poff(n_work, 0);
+    for (int i = 0; i < n_work; ++i) {
+      const int id = warp_ids[i];
+      if (id < 0) continue;
+      const Plan &p = c->groups[work[i].group]->plan;
+      if (id >= (int)c->warps.size() || warp_dim(c, id) != p.D)
+        return c->fail(QIW_ERR_ARG, "qiw_integrate_warped: warp id invalid or of the wrong dimension");
+      poff[i] = total;
+      total += (size_t)t.works[i].n_samples * (p.D + 1);
+    }
+    if (total > 0) {
+      if ((rc = c->cuda(c->d_pts.reserve(total), "alloc warped points"))) return rc;
+      for (int i = 0; i < n_work; ++i) {
+        if (warp_ids[i] < 0) continue;
+        double *dst = c->d_pts.p + poff[i];
+        if ((rc = warp_map_device(c, warp_ids[i], t.works[i].m, t.works[i].x0, t.works[i].first_index,
+                                  t.works[i].n_samples, dst)))
+          return rc;
+        t.works[i].pts = dst;
+      }
+    }
+  }
+  if (sample_out) {
+    const size_t n = (size_t)t.works[0].n_samples * t.res_sizes[0];
+    if ((rc = c->cuda(c->d_samples.reserve(n), "alloc samples")) ||
+        (rc = c->cuda(cudaMemsetAsync(c->d_samples.p, 0, sizeof(double) * n, st), "clear samples")))
+      return rc;
+    t.works[0].sample_out = c->d_samples.p;
+  }
+  const int n_cta = (int)t.cta_map.size();
+  int zero = 0;
+  if ((rc = c->cuda(c->d_works.upload(t.works.data(), t.works.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_cta_map.upload(t.cta_map.data(), t.cta_map.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_cta_first.upload(t.cta_first.data(), t.cta_first.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_res_sizes.upload(t.res_sizes.data(), t.res_sizes.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_out_off.upload(t.out_off.data(), t.out_off.size(), st), "upload work")) ||
+      (rc = c->cuda(c->d_err.upload(&zero, 1, st), "upload work")) ||
+      (rc = c->cuda(c->d_partials.reserve((size_t)n_cta * t.res_max), "alloc partials")) ||
+      (rc = c->cuda(c->d_out.reserve((size_t)2 * t.out_total), "alloc out")))
+    return rc;
+  rc = launch_tables(c, t, precision, c->d_groups.p, c->d_works.p, c->d_cta_map.p, c->d_cta_first.p,
+                     c->d_res_sizes.p, c->d_out_off.p, c->d_partials.p, c->d_err.p, c->d_out.p);
+  if (rc) return rc;
+  int err_word = 0;
+  if ((rc = c->cuda(cudaMemcpyAsync(out, c->d_out.p, sizeof(double) * 2 * t.out_total, cudaMemcpyDeviceToHost, st), "copy out")) ||
+      (rc = c->cuda(cudaMemcpyAsync(&err_word, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "copy err")))
+    return rc;
+  if (sample_out &&
+      (rc = c->cuda(cudaMemcpyAsync(sample_out, c->d_samples.p,
+                                    sizeof(double) * (size_t)t.works[0].n_samples * t.res_sizes[0],
+                                    cudaMemcpyDeviceToHost, st), "copy samples")))
+    return rc;
+  if ((rc = c->cuda(cudaStreamSynchronize(st), "integrate"))) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->last_ms = ms;
+  if (err_word) return c->fail(QIW_ERR_DEVICE, "qiw_integrate: non-finite result detected on the device");
+  return QIW_OK;
+}
+
 int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, LaunchTables *t) {
   if (precision != QIW_PREC_FP64 && precision != QIW_PREC_FP32)
     return c->fail(QIW_ERR_ARG, "qiw_integrate: unknown precision");
@@ -193,7 +271,10 @@ void qiw_ctx_destroy(qiw_ctx *c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   c->clear_groups();
+  destroy_warps(c);
   c->d_groups.release();
+  c->d_pts.release();
+  c->d_samples.release();
   for (auto *b : {&c->d_dims, &c->d_ptab_off, &c->d_eoff, &c->d_res_off, &c->d_delta_kind, &c->d_delta_off,
                   &c->d_cta_first, &c->d_res_sizes, &c->d_out_off, &c->d_err})
     b->release();
@@ -396,43 +477,17 @@ int qiw_group_stats_get(qiw_ctx *c, int32_t gid, qiw_group_stats *out) {
 }
 
 int qiw_integrate(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, double *out) {
-  if (!c || n_work < 0 || (n_work > 0 && (!work || !out))) return QIW_ERR_ARG;
-  cudaSetDevice(c->device);
-  if (n_work == 0) return QIW_OK;
-  LaunchTables t;
-  int rc = prepare_launch(c, n_work, work, precision, &t);
-  if (rc) return rc;
-  if ((rc = sync_groups(c))) return rc;
-  cudaStream_t st = c->stream;
-  if ((rc = c->cuda(c->d_sobol.upload(t.sobol.data(), t.sobol.size(), st), "upload Sobol"))) return rc;
-  for (auto &w : t.works) {
-    w.m = c->d_sobol.p + (uintptr_t)w.m;
-    w.x0 = c->d_sobol.p + (uintptr_t)w.x0;
-  }
-  const int n_cta = (int)t.cta_map.size();
-  int zero = 0;
-  if ((rc = c->cuda(c->d_works.upload(t.works.data(), t.works.size(), st), "upload work")) ||
-      (rc = c->cuda(c->d_cta_map.upload(t.cta_map.data(), t.cta_map.size(), st), "upload work")) ||
-      (rc = c->cuda(c->d_cta_first.upload(t.cta_first.data(), t.cta_first.size(), st), "upload work")) ||
-      (rc = c->cuda(c->d_res_sizes.upload(t.res_sizes.data(), t.res_sizes.size(), st), "upload work")) ||
-      (rc = c->cuda(c->d_out_off.upload(t.out_off.data(), t.out_off.size(), st), "upload work")) ||
-      (rc = c->cuda(c->d_err.upload(&zero, 1, st), "upload work")) ||
-      (rc = c->cuda(c->d_partials.reserve((size_t)n_cta * t.res_max), "alloc partials")) ||
-      (rc = c->cuda(c->d_out.reserve((size_t)2 * t.out_total), "alloc out")))
-    return rc;
-  rc = launch_tables(c, t, precision, c->d_groups.p, c->d_works.p, c->d_cta_map.p, c->d_cta_first.p, c->d_res_sizes.p,
-                     c->d_out_off.p, c->d_partials.p, c->d_err.p, c->d_out.p);
-  if (rc) return rc;
-  int err_word = 0;
-  if ((rc = c->cuda(cudaMemcpyAsync(out, c->d_out.p, sizeof(double) * 2 * t.out_total, cudaMemcpyDeviceToHost, st), "copy out")) ||
-      (rc = c->cuda(cudaMemcpyAsync(&err_word, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "copy err")) ||
-      (rc = c->cuda(cudaStreamSynchronize(st), "integrate")))
-    return rc;
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-  c->last_ms = ms;
-  if (err_word) return c->fail(QIW_ERR_DEVICE, "qiw_integrate: non-finite result detected on the device");
-  return QIW_OK;
+  return integrate_impl(c, n_work, work, precision, out, nullptr, nullptr);
+}
+
+int qiw_integrate_warped(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, const int32_t *warp_ids,
+                         int32_t precision, double *out) {
+  return integrate_impl(c, n_work, work, precision, out, warp_ids, nullptr);
+}
+
+int qiw_integrate_samples(qiw_ctx *c, const qiw_work_desc *work, int32_t precision, double *out, double *samples) {
+  if (!c || !work || !samples) return QIW_ERR_ARG;
+  return integrate_impl(c, 1, work, precision, out, nullptr, samples);
 }
 
 int qiw_measure_fma_peak(qiw_ctx *c, int32_t precision, double *tflops) {

@@ -48,6 +48,8 @@ struct GroupRec {
   DevGroup dg;
 };
 
+struct WarpRec;
+
 // Host-side launch tables of one qiw_integrate call.
 struct LaunchTables {
   std::vector<DevWork> works;         // Sobol pointers hold offsets into `sobol` until placed
@@ -90,6 +92,8 @@ struct qiw_ctx {
   qiw::DevBuf<double> d_partials, d_out;
   qiw::DevBuf<int> d_cta_first, d_res_sizes, d_out_off, d_err;
   qiw::DevBuf<uint32_t> d_sobol;
+  qiw::DevBuf<double> d_pts, d_samples;
+  std::vector<qiw::WarpRec *> warps;
   int threads = 64;
 
   int fail(int code, const std::string &msg) {
@@ -141,6 +145,14 @@ namespace qiw {
 int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, LaunchTables *t);
 // Uploads the group descriptor table if groups changed.
 int sync_groups(qiw_ctx *c);
+// Learned warps (csrc/qiw_warp.cu).
+void destroy_warps(qiw_ctx *c);
+int warp_dim(qiw_ctx *c, int id);
+int warp_map_device(qiw_ctx *c, int id, const uint32_t *m_dev, const uint32_t *x0_dev, uint64_t first, uint64_t n,
+                    double *pts_dev);
+// qiw_integrate with optional learned warps per work item and optional per-sample results.
+int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, double *out,
+                   const int32_t *warp_ids, double *sample_out);
 // Launches the kernels on launch tables already in device memory (timed by ev0/ev1).
 int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const DevGroup *groups, const DevWork *works,
                   const int4 *cta_map, const int *cta_first, const int *res_sizes, const int *out_off,

@@ -76,6 +76,8 @@ struct DevWork {
   uint64_t n_samples;
   const uint32_t *m;           // [D][32]
   const uint32_t *x0;          // [D]
+  const double *pts;           // optional [n_samples][D + 1]: warped points x and weights 1/q(x)
+  double *sample_out;          // optional [n_samples][res_size]: per-sample integrand values
 };
 
 // Device view of the problem data.  Tables hold i*P and i*Delta (real in the

@@ -299,6 +299,7 @@ __global__ void __launch_bounds__(kMaxThreads, kMinBlocks)
 #pragma unroll 1
   for (int e = 0; e < res_size; ++e) R[e] = 0.0;
 
+  double wt = 1.0;
   if (active) {
     double tm[kMaxNodes];
     const double tsel[3] = {w.t_i, w.t_w, w.t_f};
@@ -310,13 +311,21 @@ __global__ void __launch_bounds__(kMaxThreads, kMinBlocks)
       const uint32_t gray = (uint32_t)(n ^ (n >> 1));
       double u[kMaxDim];
 #pragma unroll 1
-      for (int d = 0; d < D; ++d) {
-        uint32_t v = __ldg(w.x0 + d);
-        const uint32_t *md = w.m + d * 32;
+      if (w.pts) {  // warped point x = w(y) of a learned change of variables, weight 1/q(x)
+        const double *pp = w.pts + sidx * (uint64_t)(D + 1);
+#pragma unroll 1
+        for (int d = 0; d < D; ++d) u[d] = pp[d];
+        wt = pp[D];
+      } else {
+#pragma unroll 1
+        for (int d = 0; d < D; ++d) {
+          uint32_t v = __ldg(w.x0 + d);
+          const uint32_t *md = w.m + d * 32;
 #pragma unroll 8
-        for (int b = 0; b < 32; ++b)
-          if ((gray >> b) & 1u) v ^= __ldg(md + b);
-        u[d] = ldexp((double)v, -32);  // exact: ldexp(Float64(x), -32)
+          for (int b = 0; b < 32; ++b)
+            if ((gray >> b) & 1u) v ^= __ldg(md + b);
+          u[d] = ldexp((double)v, -32);  // exact: ldexp(Float64(x), -32)
+        }
       }
       if (g.kind == 1) {  // RootTransform over [t_i, t_f]
         const double u_diff = w.t_f - w.t_i;
@@ -412,6 +421,14 @@ __global__ void __launch_bounds__(kMaxThreads, kMinBlocks)
     for (int ip = i0; ip < i1; ++ip) {
       const Instr I = load_instr(g.ins + ip);
       exec_instr<T, RESMAX>(I, A, O, R);
+    }
+    if (w.pts) {
+#pragma unroll 1
+      for (int e = 0; e < res_size; ++e) R[e] *= wt;
+    }
+    if (w.sample_out) {  // per-sample values (batches of one sample add up)
+#pragma unroll 1
+      for (int e = 0; e < res_size; ++e) atomicAdd(w.sample_out + sidx * (uint64_t)res_size + e, R[e]);
     }
   }
 

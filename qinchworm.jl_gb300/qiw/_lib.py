@@ -30,7 +30,9 @@ QIW_PREC_FP32 = 1
 
 EXPORTS = ["qiw_ctx_create", "qiw_ctx_destroy", "qiw_last_error", "qiw_problem_set", "qiw_ppgf_set",
            "qiw_group_create", "qiw_group_stats_get", "qiw_integrate", "qiw_last_kernel_ms",
-           "qiw_measure_fma_peak", "qiw_integrate_noalloc"]
+           "qiw_measure_fma_peak", "qiw_integrate_noalloc", "qiw_warp_create", "qiw_warp_set_mix", "qiw_warp_n_params",
+           "qiw_warp_get_params", "qiw_warp_set_params", "qiw_warp_grad", "qiw_warp_train", "qiw_warp_map",
+           "qiw_integrate_warped", "qiw_integrate_samples"]
 
 
 class ProblemDesc(C.Structure):
@@ -84,6 +86,19 @@ def load(path: Optional[str] = None) -> C.CDLL:
     lib.qiw_last_kernel_ms.restype = C.c_double
     lib.qiw_measure_fma_peak.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
     lib.qiw_integrate_noalloc.argtypes = [C.c_void_p, C.c_int32, C.POINTER(WorkDesc), C.c_int32, C.c_void_p]
+    lib.qiw_warp_create.argtypes = [C.c_void_p, C.c_int32, C.c_uint64, C.POINTER(C.c_int32)]
+    lib.qiw_warp_set_mix.argtypes = [C.c_void_p, C.c_int32, C.c_double]
+    lib.qiw_warp_n_params.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]
+    lib.qiw_warp_get_params.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+    lib.qiw_warp_set_params.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+    lib.qiw_warp_grad.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                  C.POINTER(C.c_double)]
+    lib.qiw_warp_train.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32,
+                                   C.c_double, C.POINTER(C.c_double)]
+    lib.qiw_warp_map.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_void_p]
+    lib.qiw_integrate_warped.argtypes = [C.c_void_p, C.c_int32, C.POINTER(WorkDesc), C.c_void_p, C.c_int32,
+                                         C.c_void_p]
+    lib.qiw_integrate_samples.argtypes = [C.c_void_p, C.POINTER(WorkDesc), C.c_int32, C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
 

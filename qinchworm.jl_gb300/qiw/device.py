@@ -86,8 +86,7 @@ class Device:
         return self._sobol_cache[D]
 
     # -- integration --------------------------------------------------------------
-    def integrate(self, works: Sequence[Work], precision: int = _lib.QIW_PREC_FP64) -> List[List[np.ndarray]]:
-        """Runs all work items in one launch; returns per item the list of sector blocks."""
+    def _descs(self, works):
         descs = (_lib.WorkDesc * len(works))()
         keep = []
         for i, w in enumerate(works):
@@ -100,19 +99,89 @@ class Device:
             keep += [m, x0]
             descs[i] = _lib.WorkDesc(w.group, 0, w.t_i, w.t_w, w.t_f, w.first_index, w.n_samples,
                                      w.n_total or w.n_samples, m.ctypes.data, x0.ctypes.data)
+        return descs, keep
+
+    def _unpack(self, out, n):
         dims = self.packed.dims
         rs = int(np.sum(dims ** 2))
-        out = np.zeros(2 * rs * len(works))
-        self._check(self.lib.qiw_integrate(self.h, len(works), descs, precision, out.ctypes.data))
         res = []
         z = out[0::2] + 1j * out[1::2]
-        for i in range(len(works)):
+        for i in range(n):
             blocks, o = [], i * rs
             for d in dims:
                 blocks.append(z[o:o + d * d].reshape(d, d, order="F").copy())
                 o += d * d
             res.append(blocks)
         return res
+
+    def integrate(self, works: Sequence[Work], precision: int = _lib.QIW_PREC_FP64,
+                  warps: Optional[Sequence[int]] = None) -> List[List[np.ndarray]]:
+        """Runs all work items in one launch; returns per item the list of sector blocks.
+        `warps[i]` >= 0 evaluates item i on the points of that learned warp."""
+        descs, keep = self._descs(works)
+        dims = self.packed.dims
+        rs = int(np.sum(dims ** 2))
+        out = np.zeros(2 * rs * len(works))
+        if warps is None:
+            self._check(self.lib.qiw_integrate(self.h, len(works), descs, precision, out.ctypes.data))
+        else:
+            ids = np.ascontiguousarray(warps, dtype=np.int32)
+            self._check(self.lib.qiw_integrate_warped(self.h, len(works), descs, ids.ctypes.data, precision,
+                                                      out.ctypes.data))
+        return self._unpack(out, len(works))
+
+    def integrate_samples(self, work: Work, precision: int = _lib.QIW_PREC_FP64):
+        """One work item; returns (blocks, per-sample values [n_samples][sum d^2])."""
+        descs, keep = self._descs([work])
+        rs = int(np.sum(self.packed.dims ** 2))
+        out = np.zeros(2 * rs)
+        samples = np.zeros((work.n_samples, rs))
+        self._check(self.lib.qiw_integrate_samples(self.h, descs, precision, out.ctypes.data, samples.ctypes.data))
+        return self._unpack(out, 1)[0], samples
+
+    # -- learned warps --------------------------------------------------------------
+    def warp_create(self, D: int, seed: int = 0, uniform_mix: Optional[float] = None) -> int:
+        wid = C.c_int32()
+        self._check(self.lib.qiw_warp_create(self.h, D, seed, C.byref(wid)))
+        if uniform_mix is not None:
+            self._check(self.lib.qiw_warp_set_mix(self.h, wid.value, uniform_mix))
+        return wid.value
+
+    def warp_params(self, wid: int) -> np.ndarray:
+        n = C.c_int64()
+        self._check(self.lib.qiw_warp_n_params(self.h, wid, C.byref(n)))
+        p = np.zeros(n.value)
+        self._check(self.lib.qiw_warp_get_params(self.h, wid, p.ctypes.data))
+        return p
+
+    def warp_set_params(self, wid: int, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        self._check(self.lib.qiw_warp_set_params(self.h, wid, p.ctypes.data))
+
+    def warp_grad(self, wid: int, x: np.ndarray, w: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        g = np.zeros_like(self.warp_params(wid))
+        loss = C.c_double()
+        self._check(self.lib.qiw_warp_grad(self.h, wid, x.ctypes.data, w.ctypes.data, len(w), g.ctypes.data,
+                                           C.byref(loss)))
+        return g, loss.value
+
+    def warp_train(self, wid: int, x: np.ndarray, w: np.ndarray, steps: int = 400, batch: int = 4096,
+                   lr: float = 3e-3) -> float:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        loss = C.c_double()
+        self._check(self.lib.qiw_warp_train(self.h, wid, x.ctypes.data, w.ctypes.data, len(w), steps, batch, lr,
+                                            C.byref(loss)))
+        return loss.value
+
+    def warp_map(self, wid: int, D: int, first: int, n: int, m=None, x0=None) -> np.ndarray:
+        m = np.ascontiguousarray(self.sobol(D) if m is None else m, dtype=np.uint32)
+        x0 = np.ascontiguousarray(np.zeros(D, np.uint32) if x0 is None else x0, dtype=np.uint32)
+        pts = np.zeros((n, D + 1))
+        self._check(self.lib.qiw_warp_map(self.h, wid, m.ctypes.data, x0.ctypes.data, first, n, pts.ctypes.data))
+        return pts
 
     def fma_peak_tflops(self, precision: int = _lib.QIW_PREC_FP64) -> float:
         v = C.c_double()

@@ -149,3 +149,15 @@ class ScrambledSobolSeq:
             g >>= 1
             b += 1
         return x
+
+
+def sobol_points(m: np.ndarray, first: int, n: int, x0: Optional[np.ndarray] = None) -> np.ndarray:
+    """Points first .. first+n-1 in [0, 1)^D (rows), by the Gray-code jump of point_uint."""
+    D = m.shape[0]
+    idx = np.arange(first, first + n, dtype=np.uint64)
+    g = idx ^ (idx >> np.uint64(1))
+    x = np.broadcast_to(np.zeros(D, np.uint32) if x0 is None else np.asarray(x0, np.uint32), (n, D)).copy()
+    for b in range(32):
+        sel = ((g >> np.uint64(b)) & np.uint64(1)).astype(bool)
+        x[sel] ^= m[:, b].astype(np.uint32)
+    return np.ldexp(x.astype(np.float64), -32)
