@@ -416,6 +416,13 @@ int qiw_group_create(qiw_ctx *c, const qiw_group_desc *d, int32_t *group_id) {
   GroupRec *g = new GroupRec();
   std::string e;
   int rc = plan_group(c->hp, gs, opt, &g->plan, &e);
+  if (rc == QIW_ERR_MEMORY && opt.arena_budget == kArenaLarge) {
+    // large sector blocks: one (topology, sector) tree needs more than the large arena
+    opt.arena_budget = kArenaHuge;
+    e.clear();
+    g->plan = Plan();
+    rc = plan_group(c->hp, gs, opt, &g->plan, &e);
+  }
   if (rc) {
     delete g;
     return c->fail(rc, "qiw_group_create: " + e);

@@ -509,6 +509,7 @@ static cudaError_t launch_t(const LaunchArgs &a) {
 int arena_class(int64_t arena) {
   if (arena <= kArenaSmall) return 0;
   if (arena <= kArenaLarge) return 1;
+  if (arena <= kArenaHuge) return 2;
   return -1;
 }
 
@@ -517,9 +518,11 @@ cudaError_t launch_eval(const LaunchArgs &a) {
   const int ac = arena_class(a.arena_max);
   if (a.fp32) {
     if (ac == 0) return big_res ? launch_t<float, kArenaSmall, kResLarge>(a) : launch_t<float, kArenaSmall, kResSmall>(a);
+    if (ac == 2) return launch_t<float, kArenaHuge, kResLarge>(a);
     return big_res ? launch_t<float, kArenaLarge, kResLarge>(a) : launch_t<float, kArenaLarge, kResSmall>(a);
   }
   if (ac == 0) return big_res ? launch_t<double, kArenaSmall, kResLarge>(a) : launch_t<double, kArenaSmall, kResSmall>(a);
+  if (ac == 2) return launch_t<double, kArenaHuge, kResLarge>(a);
   return big_res ? launch_t<double, kArenaLarge, kResLarge>(a) : launch_t<double, kArenaLarge, kResSmall>(a);
 }
 

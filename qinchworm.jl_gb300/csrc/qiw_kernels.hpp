@@ -15,6 +15,7 @@ constexpr int kMaxThreads = 128;     // samples per CTA (upper bound)
 constexpr int kMinBlocks = QIW_MIN_BLOCKS;  // 128-thread blocks per SM the register budget allows
 constexpr int kArenaSmall = 1024;    // per-sample arena instantiations (elements)
 constexpr int kArenaLarge = 8192;
+constexpr int kArenaHuge = 20480;   // large-sector problems (9x9 blocks); results always kResLarge
 constexpr int kResSmall = 64;        // result-size instantiations (sum of d_s^2)
 constexpr int kResLarge = 512;
 
@@ -43,7 +44,7 @@ struct FinishArgs {
   cudaStream_t stream;
 };
 
-int arena_class(int64_t arena);   // 0 small, 1 large, -1 too large
+int arena_class(int64_t arena);   // 0 small, 1 large, 2 huge, -1 too large
 cudaError_t launch_eval(const LaunchArgs &a);
 cudaError_t launch_finish(const FinishArgs &a);
 cudaError_t launch_fma_peak(bool fp32, void *out, int blocks, int threads, int iters, cudaStream_t st);

@@ -195,3 +195,27 @@ def test_fp32_path_errors_are_stated_and_small(device):
     dG = np.abs(res[0][1] - res[1][1]).max()
     print(f"FP32 vs FP64: max|dP| = {dP:.2e}, max|dG| = {dG:.2e}")
     assert dP < 1e-5 and dG < 1e-5
+
+
+T2G_CASES = [(_lib.QIW_GROUP_BOLD, 1, 1, 64), (_lib.QIW_GROUP_BOLD, 2, 2, 64), (_lib.QIW_GROUP_BOLD, 3, 1, 12),
+             (_lib.QIW_GROUP_BOLD, 3, 3, 12), (_lib.QIW_GROUP_CORRELATOR, 2, 2, 32),
+             (_lib.QIW_GROUP_CORRELATOR, 3, 3, 8)]
+
+
+@pytest.mark.parametrize("kind,order,npa,N", T2G_CASES)
+def test_t2g_groups_match_oracle(device, kind, order, npa, N):
+    """Three-orbital t2g model: sector blocks up to 9x9, order-3 groups on the largest arena."""
+    exp = models.t2g_bethe(n_tau=64, corr=True)
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    tops = _tops(kind, order, npa)
+    corr = 1 if kind == _lib.QIW_GROUP_CORRELATOR else None
+    gid = device.create_group(kind, order, npa, tops, corr)
+    t = (g.tau(0), g.tau(40), g.tau(41)) if kind == _lib.QIW_GROUP_BOLD else (g.tau(0), g.tau(23), g.tau(63))
+    got = device.integrate([Work(gid, *t, 0, N, N)])[0]
+    want = orc.OracleProblem(exp).integrate(_okind(kind), order, npa, [(x.pairs, x.parity) for x in tops],
+                                            *t, N, corr=corr)
+    assert _rel(got, want) < REL64
+    got32 = device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32)[0]
+    assert _rel(got32, want) < REL32
