@@ -186,6 +186,55 @@ double qiw_last_kernel_ms(const qiw_ctx *ctx);
  * every SM, the roofline denominator of the evaluation kernels. */
 int qiw_measure_fma_peak(qiw_ctx *ctx, int32_t precision, double *tflops);
 
+/* ---- Batched independent solves.  No counterpart in the reference, which runs one
+ * inchworm! per process.  A solve is one whole inchworm! loop (src/inchworm.jl:332-498 with
+ * one unscrambled Sobol sequence and one rank): the bare step tau_0 -> tau_1
+ * (inchworm_step_bare, :431-447), then bold steps n = 1 .. n_steps (inchworm_step, :474-493),
+ * each followed by set_ppgf! and normalize!(P, tau_{n+1}).  All solves of a batch share one
+ * launch queue per step -- a persistent kernel over the tiles of every (solve, group) --
+ * and the loop, P update included, runs on the device, optionally as one CUDA graph. */
+typedef struct qiw_batch qiw_batch;
+
+typedef struct {
+  const qiw_problem_desc *problem;
+  const double *taus;           /* [n_tau] grid times */
+  const double *P_init;         /* initial P (atomic), interleaved complex, layout of qiw_ppgf_set */
+  int32_t n_bare, n_bold;
+  const qiw_group_desc *bare;   /* groups of the bare step */
+  const qiw_group_desc *bold;   /* groups of every bold step, by ascending order */
+  uint64_t n_samples;           /* qMC points per group and step: a power of 2, <= 2^32 */
+  int32_t n_steps;              /* bold steps, 0 .. n_tau - 2 */
+  int32_t reserved;
+} qiw_solve_desc;
+
+#define QIW_BATCH_GRAPH 1       /* capture the whole loop in one CUDA graph and launch that */
+#define QIW_BATCH_AUTOTUNE 2    /* time tile sizes and grids on one step first, keep the fastest */
+
+typedef struct {
+  double kernel_ms;             /* device time of the last run, all steps */
+  double flops;                 /* algorithmic flops of the last run (planner counts) */
+  double topology_samples;      /* (topology, qMC sample) evaluations of the last run */
+  int32_t threads;              /* samples per tile (threads per CTA) */
+  int32_t grid;                 /* CTAs of each evaluation launch */
+  int32_t persistent;           /* 1: grid = resident CTAs, 0: one CTA per tile */
+  int32_t n_steps_max;
+  int32_t graph_nodes;          /* 0 without QIW_BATCH_GRAPH */
+  int32_t n_plans;              /* distinct group programs (shared by solves) */
+  int64_t n_tiles_bold, n_tiles_bare;
+  double tune_ms[6];            /* autotuner: step time of (threads 32, 64, 128) x (persistent, one per tile) */
+} qiw_batch_stats;
+
+int qiw_batch_create(qiw_batch **out, int device);
+void qiw_batch_destroy(qiw_batch *b);
+const char *qiw_batch_last_error(const qiw_batch *b);
+int qiw_batch_add(qiw_batch *b, const qiw_solve_desc *solve, int32_t *solve_id);
+/* Runs every solve from its P_init.  sobol_m: [sobol_dims][32] direction numbers, enough rows
+ * for the highest order (2 * order <= sobol_dims). */
+int qiw_batch_run(qiw_batch *b, int32_t precision, int32_t flags, const uint32_t *sobol_m, int32_t sobol_dims);
+/* P of a solve after the last run, interleaved complex, layout of qiw_ppgf_set. */
+int qiw_batch_get_P(qiw_batch *b, int32_t solve_id, double *P);
+int qiw_batch_stats_get(const qiw_batch *b, qiw_batch_stats *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -244,6 +244,72 @@ int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const De
 
 }  // namespace qiw
 
+namespace qiw {
+
+// Plans a group on c's problem, uploads its program and fills its device descriptor.
+int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
+  PlanOptions opt;
+  opt.arena_budget = kArenaLarge;
+  if (const char *b = std::getenv("QIW_ARENA_BUDGET")) opt.arena_budget = std::max<int64_t>(256, std::atoll(b));
+  opt.arena_budget = std::min<int64_t>(opt.arena_budget, kArenaLarge);
+  GroupRec *g = new GroupRec();
+  std::string e;
+  int rc = plan_group(c->hp, gs, opt, &g->plan, &e);
+  if (rc == QIW_ERR_MEMORY && opt.arena_budget == kArenaLarge) {
+    // large sector blocks: one (topology, sector) tree needs more than the large arena
+    opt.arena_budget = kArenaHuge;
+    e.clear();
+    g->plan = Plan();
+    rc = plan_group(c->hp, gs, opt, &g->plan, &e);
+  }
+  if (rc) {
+    delete g;
+    return c->fail(rc, "qiw_group_create: " + e);
+  }
+  if (arena_class(g->plan.arena) < 0) {
+    delete g;
+    return c->fail(QIW_ERR_MEMORY, "qiw_group_create: per-sample arena above the largest kernel instantiation");
+  }
+  const Plan &p = g->plan;
+  if ((rc = c->cuda(g->pm.upload(p.pm.data(), p.pm.size(), c->stream), "upload plan")) ||
+      (rc = c->cuda(g->wj.upload(p.wj.data(), p.wj.size(), c->stream), "upload plan")) ||
+      (rc = c->cuda(g->ins.upload(p.ins.data(), p.ins.size(), c->stream), "upload plan")) ||
+      (rc = c->cuda(g->batch.upload(p.batch_begin.data(), p.batch_begin.size(), c->stream), "upload plan")) ||
+      (rc = c->cuda(cudaStreamSynchronize(c->stream), "upload plan"))) {
+    delete g;
+    return rc;
+  }
+  DevGroup &dg = g->dg;
+  std::memset(&dg, 0, sizeof(dg));
+  dg.kind = p.kind;
+  dg.order = p.order;
+  dg.n_nodes = p.n_nodes;
+  dg.D = p.D;
+  dg.d_before = p.d_before;
+  dg.d_after = p.d_after;
+  dg.use_bold = p.use_bold;
+  dg.n_fixed = p.n_fixed;
+  for (int f = 0; f < p.n_fixed; ++f) {
+    dg.fixed_pos[f] = p.fixed_pos[f];
+    dg.fixed_time[f] = p.fixed_time[f];
+  }
+  for (size_t j = 0; j < p.var_pos.size(); ++j) dg.var_pos[j] = p.var_pos[j];
+  dg.n_pm = (int)p.pm.size();
+  dg.n_w = (int)p.wj.size();
+  dg.n_instr = (int)p.ins.size();
+  dg.arena = (int)p.arena;
+  dg.res_size = p.res_size;
+  dg.n_batches = (int)p.batch_begin.size() - 1;
+  dg.pm = g->pm.p;
+  dg.wj = g->wj.p;
+  dg.ins = g->ins.p;
+  dg.batch_begin = g->batch.p;
+  *out = g;
+  return QIW_OK;
+}
+
+}  // namespace qiw
+
 extern "C" {
 
 int qiw_ctx_create(qiw_ctx **out, int device) {
@@ -409,62 +475,9 @@ int qiw_group_create(qiw_ctx *c, const qiw_group_desc *d, int32_t *group_id) {
     int grc = group_spec_from_desc(d, &gs, &e);
     if (grc) return c->fail(grc, "qiw_group_create: " + e);
   }
-  PlanOptions opt;
-  opt.arena_budget = kArenaLarge;
-  if (const char *b = std::getenv("QIW_ARENA_BUDGET")) opt.arena_budget = std::max<int64_t>(256, std::atoll(b));
-  opt.arena_budget = std::min<int64_t>(opt.arena_budget, kArenaLarge);
-  GroupRec *g = new GroupRec();
-  std::string e;
-  int rc = plan_group(c->hp, gs, opt, &g->plan, &e);
-  if (rc == QIW_ERR_MEMORY && opt.arena_budget == kArenaLarge) {
-    // large sector blocks: one (topology, sector) tree needs more than the large arena
-    opt.arena_budget = kArenaHuge;
-    e.clear();
-    g->plan = Plan();
-    rc = plan_group(c->hp, gs, opt, &g->plan, &e);
-  }
-  if (rc) {
-    delete g;
-    return c->fail(rc, "qiw_group_create: " + e);
-  }
-  if (arena_class(g->plan.arena) < 0) {
-    delete g;
-    return c->fail(QIW_ERR_MEMORY, "qiw_group_create: per-sample arena above the largest kernel instantiation");
-  }
-  const Plan &p = g->plan;
-  if ((rc = c->cuda(g->pm.upload(p.pm.data(), p.pm.size(), c->stream), "upload plan")) ||
-      (rc = c->cuda(g->wj.upload(p.wj.data(), p.wj.size(), c->stream), "upload plan")) ||
-      (rc = c->cuda(g->ins.upload(p.ins.data(), p.ins.size(), c->stream), "upload plan")) ||
-      (rc = c->cuda(g->batch.upload(p.batch_begin.data(), p.batch_begin.size(), c->stream), "upload plan")) ||
-      (rc = c->cuda(cudaStreamSynchronize(c->stream), "upload plan"))) {
-    delete g;
-    return rc;
-  }
-  DevGroup &dg = g->dg;
-  std::memset(&dg, 0, sizeof(dg));
-  dg.kind = p.kind;
-  dg.order = p.order;
-  dg.n_nodes = p.n_nodes;
-  dg.D = p.D;
-  dg.d_before = p.d_before;
-  dg.d_after = p.d_after;
-  dg.use_bold = p.use_bold;
-  dg.n_fixed = p.n_fixed;
-  for (int f = 0; f < p.n_fixed; ++f) {
-    dg.fixed_pos[f] = p.fixed_pos[f];
-    dg.fixed_time[f] = p.fixed_time[f];
-  }
-  for (size_t j = 0; j < p.var_pos.size(); ++j) dg.var_pos[j] = p.var_pos[j];
-  dg.n_pm = (int)p.pm.size();
-  dg.n_w = (int)p.wj.size();
-  dg.n_instr = (int)p.ins.size();
-  dg.arena = (int)p.arena;
-  dg.res_size = p.res_size;
-  dg.n_batches = (int)p.batch_begin.size() - 1;
-  dg.pm = g->pm.p;
-  dg.wj = g->wj.p;
-  dg.ins = g->ins.p;
-  dg.batch_begin = g->batch.p;
+  GroupRec *g = nullptr;
+  int rc = build_group(c, gs, &g);
+  if (rc) return rc;
   c->groups.push_back(g);
   c->groups_dirty = true;
   *group_id = (int32_t)c->groups.size() - 1;

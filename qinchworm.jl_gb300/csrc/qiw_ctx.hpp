@@ -143,6 +143,8 @@ struct qiw_ctx {
 namespace qiw {
 // Validates the work items and builds the launch tables (no device memory touched).
 int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, LaunchTables *t);
+// Plans a group on c's problem, uploads its program and fills its device descriptor.
+int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out);
 // Uploads the group descriptor table if groups changed.
 int sync_groups(qiw_ctx *c);
 // Learned warps (csrc/qiw_warp.cu).

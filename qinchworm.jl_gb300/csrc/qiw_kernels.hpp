@@ -44,6 +44,54 @@ struct FinishArgs {
   cudaStream_t stream;
 };
 
+// ---- batched solves (csrc/qiw_batch.cu): many independent inchworm loops in one launch queue
+
+// One (solve, group) pair; its tiles hold partial slots [slot0, slot0 + n_slots).
+struct BatchWork {
+  int32_t group, solve, order, last_step;   // last_step: last step this work item runs
+  int32_t slot0, n_slots, res_off, pad;
+  uint64_t n_samples;
+  double inv_n;                             // 1 / n_samples (one rank, one sequence)
+  const uint32_t *m, *x0;                   // Sobol tables [D][32], [D]
+};
+
+// One solve: its grid, device P tables and the ranges of its work items.
+struct BatchSolve {
+  const double *taus;     // [n_tau]
+  const double *P0;       // initial i*P table (FP64)
+  double *P;              // i*P table, FP64 (layout of DevProblem::P)
+  float *Pf;              // FP32 copy read by the FP32 kernels
+  double *lam;            // [n_tau] normalisation exponent of each step (output)
+  int32_t last_step;      // last bold step (1 .. n_tau - 2); 0: bare step only
+  int32_t bare0, bare1;   // bare work items [bare0, bare1) of the bare list
+  int32_t bold0, bold1;   // bold work items [bold0, bold1) of the bold list
+  int32_t res_size, ptab_size, n_tau;
+};
+
+struct BatchArgs {
+  const DevProblem *probs;   // [n_solves], views of the launch precision
+  const BatchSolve *solves;
+  const DevGroup *groups;
+  const BatchWork *works;    // this step's list (bare for step 0, bold otherwise)
+  const int4 *tiles;         // (work, batch, first sample, partial slot), heaviest first
+  int *ticket;               // this step's tile counter (zero before the launch)
+  double *partials;          // [slots][pstride]
+  int pstride;               // elements per partial slot (largest result size)
+  double *res;               // per work item result (i*P units) at res_off
+  int *err_word;
+  int n_tiles, n_works, n_solves, step, grid, threads;
+  int64_t arena_max;
+  int res_max;
+  bool fp32;
+  cudaStream_t stream;
+};
+
+cudaError_t launch_batch_eval(const BatchArgs &a);     // persistent evaluation of one step
+cudaError_t launch_batch_finish(const BatchArgs &a);   // per work item results of the step
+cudaError_t launch_batch_update(const BatchArgs &a);   // P(tau_{step+1}) and normalize!(P, tau)
+cudaError_t launch_batch_reset(const BatchArgs &a);    // P = P0 for every solve
+int batch_occupancy(const BatchArgs &a, int *blocks_per_sm);
+
 int arena_class(int64_t arena);   // 0 small, 1 large, 2 huge, -1 too large
 cudaError_t launch_eval(const LaunchArgs &a);
 cudaError_t launch_finish(const FinishArgs &a);

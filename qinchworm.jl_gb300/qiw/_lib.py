@@ -32,7 +32,11 @@ EXPORTS = ["qiw_ctx_create", "qiw_ctx_destroy", "qiw_last_error", "qiw_problem_s
            "qiw_group_create", "qiw_group_stats_get", "qiw_integrate", "qiw_last_kernel_ms",
            "qiw_measure_fma_peak", "qiw_integrate_noalloc", "qiw_warp_create", "qiw_warp_set_mix", "qiw_warp_n_params",
            "qiw_warp_get_params", "qiw_warp_set_params", "qiw_warp_grad", "qiw_warp_train", "qiw_warp_map",
-           "qiw_integrate_warped", "qiw_integrate_samples"]
+           "qiw_integrate_warped", "qiw_integrate_samples", "qiw_batch_create", "qiw_batch_destroy",
+           "qiw_batch_last_error", "qiw_batch_add", "qiw_batch_run", "qiw_batch_get_P", "qiw_batch_stats_get"]
+
+QIW_BATCH_GRAPH = 1
+QIW_BATCH_AUTOTUNE = 2
 
 
 class ProblemDesc(C.Structure):
@@ -62,6 +66,20 @@ class WorkDesc(C.Structure):
 
 
 _lib = None
+
+
+class SolveDesc(C.Structure):
+    _fields_ = [("problem", C.POINTER(ProblemDesc)), ("taus", C.c_void_p), ("P_init", C.c_void_p),
+                ("n_bare", C.c_int32), ("n_bold", C.c_int32), ("bare", C.POINTER(GroupDesc)),
+                ("bold", C.POINTER(GroupDesc)), ("n_samples", C.c_uint64), ("n_steps", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_double), ("flops", C.c_double), ("topology_samples", C.c_double),
+                ("threads", C.c_int32), ("grid", C.c_int32), ("persistent", C.c_int32),
+                ("n_steps_max", C.c_int32), ("graph_nodes", C.c_int32), ("n_plans", C.c_int32),
+                ("n_tiles_bold", C.c_int64), ("n_tiles_bare", C.c_int64), ("tune_ms", C.c_double * 6)]
 
 
 def load(path: Optional[str] = None) -> C.CDLL:
@@ -99,6 +117,15 @@ def load(path: Optional[str] = None) -> C.CDLL:
     lib.qiw_integrate_warped.argtypes = [C.c_void_p, C.c_int32, C.POINTER(WorkDesc), C.c_void_p, C.c_int32,
                                          C.c_void_p]
     lib.qiw_integrate_samples.argtypes = [C.c_void_p, C.POINTER(WorkDesc), C.c_int32, C.c_void_p, C.c_void_p]
+    lib.qiw_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+    lib.qiw_batch_destroy.argtypes = [C.c_void_p]
+    lib.qiw_batch_destroy.restype = None
+    lib.qiw_batch_last_error.argtypes = [C.c_void_p]
+    lib.qiw_batch_last_error.restype = C.c_char_p
+    lib.qiw_batch_add.argtypes = [C.c_void_p, C.POINTER(SolveDesc), C.POINTER(C.c_int32)]
+    lib.qiw_batch_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32]
+    lib.qiw_batch_get_P.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+    lib.qiw_batch_stats_get.argtypes = [C.c_void_p, C.POINTER(BatchStats)]
     _lib = lib
     return lib
 

@@ -111,12 +111,8 @@ def t2g_bethe(U: float = 2.3, J: float = 0.4, beta: float = 20.0, n_tau: int = 5
     Delta = V ** 2 * gf_from_dos(BetheDOS(t=D / 2), grid)
     exp = Expansion(ed, grid, _diag_pairs(labels, [Delta] * len(labels)))
     if corr:
-        # G(tau) of orbital 1 (sign as in README.md:132) and <S+(tau) S-> of the total spin
+        # G(tau) and <S+(tau) S-> of orbital 1; correlator_2p takes single monomials only
+        # (src/inchworm.jl:1003-1004), as in README.md:132-137
         exp.add_corr_operators((-op.c("up", 1), op.c_dag("up", 1)))
-        s_plus = op.c_dag("up", 1) * op.c("dn", 1)
-        s_minus = op.c_dag("dn", 1) * op.c("up", 1)
-        for o in (2, 3):
-            s_plus = s_plus + op.c_dag("up", o) * op.c("dn", o)
-            s_minus = s_minus + op.c_dag("dn", o) * op.c("up", o)
-        exp.add_corr_operators((s_plus, s_minus))
+        exp.add_corr_operators((op.c_dag("up", 1) * op.c("dn", 1), op.c_dag("dn", 1) * op.c("up", 1)))
     return exp

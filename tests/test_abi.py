@@ -11,7 +11,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 def declared():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(qiw_[a-z_0-9]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(qiw_[A-Za-z_0-9]+)\s*\(", text)))
 
 
 def test_header_and_library_exports():
@@ -37,3 +37,6 @@ def test_null_arguments_are_rejected():
     assert lib.qiw_integrate(None, 0, None, 0, None) == _lib.QIW_ERR_ARG
     assert lib.qiw_problem_set(None, None) == _lib.QIW_ERR_ARG
     assert lib.qiw_last_error(None) == b"null context"
+    assert lib.qiw_batch_add(None, None, None) == _lib.QIW_ERR_ARG
+    assert lib.qiw_batch_run(None, 0, 0, None, 0) == _lib.QIW_ERR_ARG
+    assert lib.qiw_batch_last_error(None) == b"null batch"
