@@ -48,7 +48,11 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--model", default="eg", choices=["eg", "anderson"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy"])
+    ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy", "batch"])
+    ap.add_argument("--solves", type=int, default=64, help="batch mode: independent Anderson solves")
+    ap.add_argument("--seed", type=int, default=2024, help="batch mode: parameter seed (numpy PCG64)")
+    ap.add_argument("--no-sequential", action="store_true", help="batch mode: skip the one-solve-at-a-time arm")
+    ap.add_argument("--direct", action="store_true", help="batch mode: also time direct launches (no graph)")
     ap.add_argument("--n-tau", type=int, default=32, help="accuracy mode: tau grid size")
     ap.add_argument("--n-ref", type=int, default=2 ** 15, help="accuracy mode: samples of the FP64 reference")
     ap.add_argument("--n-max", type=int, default=2 ** 13, help="accuracy mode: largest swept N")
@@ -346,11 +350,95 @@ def run_accuracy(args):
                       "reference_solve_s": t_ref, "sweep": sweep}))
 
 
+def batch_solves(seed: int, n: int):
+    """Seed-drawn Anderson solves: beta U[2, 40], n_tau U{64..512}, U U[0.5, 4], eps U[-1, 1],
+    V U[0.2, 1], D = 2, max order U{2..6}, N = 2^U{8..14} (numpy PCG64)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(n):
+        beta = float(rng.uniform(2, 40))
+        n_tau = int(rng.integers(64, 513))
+        U = float(rng.uniform(0.5, 4))
+        eps = float(rng.uniform(-1, 1))
+        V = float(rng.uniform(0.2, 1.0))
+        kmax = int(rng.integers(2, 7))
+        N = 2 ** int(rng.integers(8, 15))
+        out.append(dict(beta=beta, n_tau=n_tau, U=U, eps=eps, V=V, kmax=kmax, N=N))
+    return out
+
+
+def run_batch(args):
+    """Independent solves in one device-resident launch queue (persistent kernel, CUDA graph,
+    autotuned tiles) against the same solves one at a time through the host-driven loop."""
+    import torch
+    from qiw import _lib, models
+    from qiw.batch import Batch
+    from qiw.device import Device
+    from qiw.inchworm import inchworm
+    prec = _lib.QIW_PREC_FP32 if args.precision == "fp32" else _lib.QIW_PREC_FP64
+    specs = batch_solves(args.seed, args.solves)
+    mk = lambda p: models.anderson(eps=p["eps"], U=p["U"], D=2.0, V=p["V"], beta=p["beta"], n_tau=p["n_tau"])
+    exps = [mk(p) for p in specs]
+    t0 = time.perf_counter()
+    b = Batch(int(os.environ.get("LOCAL_RANK", "0")))
+    for e, p in zip(exps, specs):
+        b.add(e, range(0, p["kmax"] + 1), range(0, p["kmax"] + 1), p["N"])
+    setup_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    first = b.run(prec, graph=True, autotune=True)          # tunes, captures, runs
+    first_s = time.perf_counter() - t0
+    runs = []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = b.run(prec, graph=True, autotune=True)
+        P_batch = [b.P_table(i) for i in range(len(exps))]
+        runs.append((r, time.perf_counter() - t0))
+    r, wall = min(runs, key=lambda x: x[0].kernel_ms)
+    direct = b.run(prec, graph=False, autotune=True) if args.direct else None
+    line = {"mode": "batch", "metric": "topology-sample evaluations per second, independent Anderson solves",
+            "value": r.topology_samples / (r.kernel_ms * 1e-3), "unit": "topology-samples/s", "n_gpus": 1,
+            "steps": len(runs), "ms_per_step": r.kernel_ms, "higher_is_better": True, "dtype": args.precision.replace("fp", "f"),
+            "data": "synthetic", "config": {"workload": f"{len(specs)} Anderson solves, seed {args.seed}",
+                                            "ranges": "beta U[2,40], n_tau U{64..512}, U U[0.5,4], eps U[-1,1], V U[0.2,1], D=2, max order U{2..6}, N 2^U{8..14}",
+                                            "total_steps": int(sum(p["n_tau"] - 1 for p in specs))},
+            "e2e": {"value": r.topology_samples / wall, "unit": "topology-samples/s", "seconds": wall},
+            "flops": r.flops, "tflops": r.flops / (r.kernel_ms * 1e-3) / 1e12,
+            "tiles": {"threads": r.threads, "persistent": r.persistent, "grid": r.grid, "tiles_per_step": r.tiles_per_step,
+                      "autotune_ms_step1": {f"{t}{'p' if pm == 0 else '1'}": round(first.tune_ms[i * 2 + pm], 3)
+                                            for i, t in enumerate((32, 64, 128)) for pm in (0, 1)}},
+            "graph_nodes": r.graph_nodes, "n_plans": r.n_plans, "setup_s": setup_s, "first_run_s": first_s,
+            "direct_launches_ms": direct.kernel_ms if direct else None}
+    if not args.no_sequential:
+        dev = Device(int(os.environ.get("LOCAL_RANK", "0")))
+        seq_s, worst = 0.0, 0.0
+        for i, p in enumerate(specs):
+            e = mk(p)
+            init = [P_s.data.copy() for P_s in e.P]
+            inchworm(e, range(0, p["kmax"] + 1), range(0, p["kmax"] + 1), p["N"], dev=dev, precision=prec, n_steps=1)
+            for P_s, d in zip(e.P, init):   # the short run above only planned the groups
+                P_s.data[...] = d
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            inchworm(e, range(0, p["kmax"] + 1), range(0, p["kmax"] + 1), p["N"], dev=dev, precision=prec)
+            torch.cuda.synchronize()
+            seq_s += time.perf_counter() - t0
+            ref = np.concatenate([np.transpose(P_s.data, (0, 2, 1)).ravel() for P_s in e.P])
+            worst = max(worst, float(np.abs(P_batch[i] - ref).max() / np.abs(ref).max()))
+        line["sequential"] = {"value": r.topology_samples / seq_s, "unit": "topology-samples/s", "seconds": seq_s,
+                              "what": "the same solves one at a time: host loop, one qiw_integrate launch per step"}
+        line["speedup_vs_sequential"] = seq_s / wall
+        line["max_rel_diff_vs_sequential"] = worst
+    print(json.dumps(line))
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
     elif a.mode == "accuracy":
         run_accuracy(a)
+    elif a.mode == "batch":
+        run_batch(a)
     else:
         run_ours(a)

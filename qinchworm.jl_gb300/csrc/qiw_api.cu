@@ -223,6 +223,12 @@ int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const De
   la.arena_max = t.arena_max;
   la.res_max = t.res_max;
   la.fp32 = precision == QIW_PREC_FP32;
+  la.extras = false;
+  la.stage = false;
+  for (const DevWork &w : t.works) {
+    la.extras = la.extras || w.pts != nullptr || w.sample_out != nullptr;
+    la.stage = la.stage || c->groups[w.group]->dg.scalar != 0;
+  }
   la.stream = c->stream;
   FinishArgs fa;
   fa.works = works;
@@ -300,6 +306,9 @@ int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
   dg.arena = (int)p.arena;
   dg.res_size = p.res_size;
   dg.n_batches = (int)p.batch_begin.size() - 1;
+  dg.scalar = 1;
+  for (const Instr &I : p.ins)
+    if (I.rows > 1 || I.cols > 1 || I.inner > 1) dg.scalar = 0;
   dg.pm = g->pm.p;
   dg.wj = g->wj.p;
   dg.ins = g->ins.p;

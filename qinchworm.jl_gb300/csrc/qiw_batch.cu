@@ -183,6 +183,7 @@ struct Prepared {
   int64_t arena_max = 0;
   int res_max = 0, pstride = 0, max_steps = 0;
   int grid_bare = 0, grid_bold = 0;
+  bool stage = false;
 };
 
 int prepare(qiw_batch *b, int precision, const RunCfg &cfg, Prepared *pp) {
@@ -194,6 +195,8 @@ int prepare(qiw_batch *b, int precision, const RunCfg &cfg, Prepared *pp) {
     P.res_max = std::max(P.res_max, e.rec->plan.res_size);
   }
   P.pstride = std::max(1, P.res_max);
+  P.stage = false;
+  for (const PlanEntry &e : b->plans) P.stage = P.stage || e.rec->dg.scalar != 0;
   for (const SolveRec *s : b->solves) P.max_steps = std::max(P.max_steps, s->n_steps);
   const size_t slots = (size_t)std::max(P.bare.slots, P.bold.slots);
   const size_t res = (size_t)std::max(P.bare.res_total, P.bold.res_total);
@@ -213,6 +216,7 @@ int prepare(qiw_batch *b, int precision, const RunCfg &cfg, Prepared *pp) {
   a.arena_max = P.arena_max;
   a.res_max = P.res_max;
   a.fp32 = precision == QIW_PREC_FP32;
+  a.stage = P.stage;
   int occ = 0;
   if (batch_occupancy(a, &occ)) return b->fail(QIW_ERR_CUDA, "qiw_batch_run: occupancy query failed");
   int n_sm = 0;
@@ -250,6 +254,7 @@ BatchArgs step_args(qiw_batch *b, const Prepared &P, int precision, int threads,
   a.arena_max = P.arena_max;
   a.res_max = P.res_max;
   a.fp32 = precision == QIW_PREC_FP32;
+  a.stage = P.stage;
   a.stream = b->stream;
   return a;
 }

@@ -1,0 +1,584 @@
+// Device code of the qMC diagram integration (sm_103a), shared by the kernel translation units.
+//
+// One thread evaluates one qMC sample of one topology group:
+//   1. Sobol point by Gray-code jump   x = x0 ^ XOR_{b in bits(n ^ n>>1)} m[:, b]
+//      (src/scrambled_sobol.jl:158-173, bit-exact UInt32 arithmetic);
+//   2. Root / DoubleSimplexRoot map onto ordered times (src/qmc_integrate.jl:229-238, 425-449);
+//   3. i*P(t_{j+1}-t_j) blocks by linear interpolation of the P table, or the exact atomic
+//      i*P0 = exp(-dt E) for the bare step (src/topology_eval.jl:357-374,
+//      src/exact_atomic_ppgf.jl:109-118); i*Delta_p weights (src/topology_eval.jl:412-415);
+//   4. the group's program: the merged configuration DAG built by the host planner.
+// All threads of a CTA run the same (warp-uniform) instruction stream, so control flow never
+// diverges; per-sample matrices live in the thread's arena (local memory, L1 resident).
+//
+// Real-phase arithmetic: on the imaginary branch i*P, i*Delta and the operator blocks are
+// real, so every complex product of the reference has exactly zero cross terms; the host
+// verifies that and the kernels compute the real parts only (the result is -i times it).
+//
+// Reduction: per-thread sector-block sums -> warp shuffles -> CTA shared memory (fixed
+// order) -> per-CTA partials -> one CTA per work item sums its partials in order with
+// Kahan compensation.  Re-runs are bit-identical.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "qiw.h"
+#include "qiw_internal.hpp"
+#include "qiw_kernels.hpp"
+
+namespace qiw {
+
+template <typename T>
+__device__ __forceinline__ T fmaT(T a, T b, T c);
+template <>
+__device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return fma(a, b, c); }
+template <>
+__device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+__device__ __forceinline__ Instr load_instr(const Instr *p) {
+  const int4 *q = reinterpret_cast<const int4 *>(p);
+  int4 a = __ldg(q), b = __ldg(q + 1);
+  Instr I;
+  int4 *o = reinterpret_cast<int4 *>(&I);
+  o[0] = a;
+  o[1] = b;
+  return I;
+}
+
+// Dynamic shared memory of the evaluation kernels: the reduction rows [warps][RESMAX] doubles,
+// then (launches with scalar programs) two instruction chunks of blockDim.x entries.
+extern __shared__ __align__(16) unsigned char qiw_dyn_smem[];
+__host__ __device__ constexpr size_t eval_smem_bytes(int threads, int resmax, bool stage) {
+  return (size_t)((threads + 31) / 32) * resmax * sizeof(double) + (stage ? 2 * (size_t)threads * 32 : 0);
+}
+
+// Instruction staging: thread t copies instruction start + t (if < end) into dst[t] with two
+// 16-byte cp.async (Instr is 16-byte aligned, 32 bytes).
+__device__ __forceinline__ void stage_instr(Instr *dst, const Instr *src, int start, int end) {
+  const int i = start + (int)threadIdx.x;
+  if (i < end) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst + threadIdx.x);
+    const char *gp = reinterpret_cast<const char *>(src + i);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gp) : "memory");
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s + 16u), "l"(gp + 16) : "memory");
+  }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Linear interpolation of a uniform-grid table at dt >= 0 (rule of qiw/gf.py: linear_interp).
+__device__ __forceinline__ void lin_index(double dt, double inv_h, int n_tau, int *i, double *f) {
+  double x = dt * inv_h;
+  int k = (int)floor(x);
+  k = k > n_tau - 2 ? n_tau - 2 : k;
+  k = k < 0 ? 0 : k;
+  *i = k;
+  *f = x - (double)k;
+}
+
+
+// ---------------------------------------------------------------------------------------
+// Matrix instructions.  Block dimensions 1, 2 and 4 (every sector of the Anderson and eg
+// models) take fully unrolled paths: all operands are loaded into registers first, so the
+// arena reads of one instruction are in flight together, then 4..64 independent FMAs run.
+// Other dimensions use the generic loops.
+
+__device__ __forceinline__ int dcode(int d) { return d == 1 ? 0 : d == 2 ? 1 : d == 4 ? 2 : -1; }
+
+template <typename T, int R, int C>
+__device__ __forceinline__ void pmul_u(T *A, int dst, int pm, int src) {
+  T p[R * R], x[R * C];
+#pragma unroll
+  for (int i = 0; i < R * R; ++i) p[i] = A[pm + i];
+#pragma unroll
+  for (int i = 0; i < R * C; ++i) x[i] = A[src + i];
+#pragma unroll
+  for (int j = 0; j < C; ++j)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      T acc = p[r] * x[j * R];
+#pragma unroll
+      for (int k = 1; k < R; ++k) acc = fmaT<T>(p[k * R + r], x[j * R + k], acc);
+      A[dst + j * R + r] = acc;
+    }
+}
+
+template <typename T, int R, int C>
+__device__ __forceinline__ void pmuld_u(T *A, int dst, int pm, int src) {
+  T p[R], x[R * C];
+#pragma unroll
+  for (int i = 0; i < R; ++i) p[i] = A[pm + i];
+#pragma unroll
+  for (int i = 0; i < R * C; ++i) x[i] = A[src + i];
+#pragma unroll
+  for (int j = 0; j < C; ++j)
+#pragma unroll
+    for (int r = 0; r < R; ++r) A[dst + j * R + r] = p[r] * x[j * R + r];
+}
+
+// dst (=|+=) coef * O * src.  MODE 0: no coefficient (coef == 1 exactly), MODE 1: the
+// coefficient scales the smaller of src (K x C) and the product (R x C).
+template <typename T, int R, int K, int C, int MODE>
+__device__ __forceinline__ void omul_m(T *A, const T *O, int dst, int oa, int src, T coef, bool accf) {
+  T o[R * K], x[K * C];
+#pragma unroll
+  for (int i = 0; i < R * K; ++i) o[i] = __ldg(O + oa + i);
+#pragma unroll
+  for (int i = 0; i < K * C; ++i) x[i] = A[src + i];
+  constexpr bool scale_src = (MODE == 1) && (K < R);
+  if (scale_src) {
+#pragma unroll
+    for (int i = 0; i < K * C; ++i) x[i] *= coef;
+  }
+#pragma unroll
+  for (int j = 0; j < C; ++j)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int d = dst + j * R + r;
+      T acc;
+      if (accf && !(MODE == 1 && !scale_src)) {
+        // accumulate into the destination: the chain starts from its value (K FMAs)
+        acc = A[d];
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc = fmaT<T>(o[k * R + r], x[j * K + k], acc);
+      } else {
+        acc = o[r] * x[j * K];
+#pragma unroll
+        for (int k = 1; k < K; ++k) acc = fmaT<T>(o[k * R + r], x[j * K + k], acc);
+        if (MODE == 1 && !scale_src) acc = accf ? fmaT<T>(coef, acc, A[d]) : coef * acc;
+      }
+      A[d] = acc;
+    }
+}
+
+template <typename T, int R, int K, int C>
+__device__ __forceinline__ void omul_u(T *A, const T *O, int dst, int oa, int src, T coef, bool accf,
+                                       bool has_coef) {
+  if (has_coef) omul_m<T, R, K, C, 1>(A, O, dst, oa, src, coef, accf);
+  else omul_m<T, R, K, C, 0>(A, O, dst, oa, src, coef, accf);
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void axpy_u(T *A, int dst, int src, T coef, bool accf, bool has_coef) {
+  T x[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) x[i] = A[src + i];
+  if (has_coef) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) A[dst + i] = accf ? fmaT<T>(coef, x[i], A[dst + i]) : coef * x[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < N; ++i) A[dst + i] = accf ? x[i] + A[dst + i] : x[i];
+  }
+}
+
+#define QIW_D3(F, ...)                                                                            \
+  switch (code) {                                                                                 \
+    case 0: F<T, 1, 1, 1>(__VA_ARGS__); break;  case 1: F<T, 1, 1, 2>(__VA_ARGS__); break;        \
+    case 2: F<T, 1, 1, 4>(__VA_ARGS__); break;  case 3: F<T, 1, 2, 1>(__VA_ARGS__); break;        \
+    case 4: F<T, 1, 2, 2>(__VA_ARGS__); break;  case 5: F<T, 1, 2, 4>(__VA_ARGS__); break;        \
+    case 6: F<T, 1, 4, 1>(__VA_ARGS__); break;  case 7: F<T, 1, 4, 2>(__VA_ARGS__); break;        \
+    case 8: F<T, 1, 4, 4>(__VA_ARGS__); break;  case 9: F<T, 2, 1, 1>(__VA_ARGS__); break;        \
+    case 10: F<T, 2, 1, 2>(__VA_ARGS__); break; case 11: F<T, 2, 1, 4>(__VA_ARGS__); break;       \
+    case 12: F<T, 2, 2, 1>(__VA_ARGS__); break; case 13: F<T, 2, 2, 2>(__VA_ARGS__); break;       \
+    case 14: F<T, 2, 2, 4>(__VA_ARGS__); break; case 15: F<T, 2, 4, 1>(__VA_ARGS__); break;       \
+    case 16: F<T, 2, 4, 2>(__VA_ARGS__); break; case 17: F<T, 2, 4, 4>(__VA_ARGS__); break;       \
+    case 18: F<T, 4, 1, 1>(__VA_ARGS__); break; case 19: F<T, 4, 1, 2>(__VA_ARGS__); break;       \
+    case 20: F<T, 4, 1, 4>(__VA_ARGS__); break; case 21: F<T, 4, 2, 1>(__VA_ARGS__); break;       \
+    case 22: F<T, 4, 2, 2>(__VA_ARGS__); break; case 23: F<T, 4, 2, 4>(__VA_ARGS__); break;       \
+    case 24: F<T, 4, 4, 1>(__VA_ARGS__); break; case 25: F<T, 4, 4, 2>(__VA_ARGS__); break;       \
+    default: F<T, 4, 4, 4>(__VA_ARGS__); break;                                                   \
+  }
+
+#define QIW_D2(F, ...)                                                                            \
+  switch (code) {                                                                                 \
+    case 0: F<T, 1, 1>(__VA_ARGS__); break; case 1: F<T, 1, 2>(__VA_ARGS__); break;               \
+    case 2: F<T, 1, 4>(__VA_ARGS__); break; case 3: F<T, 2, 1>(__VA_ARGS__); break;               \
+    case 4: F<T, 2, 2>(__VA_ARGS__); break; case 5: F<T, 2, 4>(__VA_ARGS__); break;               \
+    case 6: F<T, 4, 1>(__VA_ARGS__); break; case 7: F<T, 4, 2>(__VA_ARGS__); break;               \
+    default: F<T, 4, 4>(__VA_ARGS__); break;                                                      \
+  }
+
+// Programs whose blocks are all 1x1 (single-orbital models): about 1.5 flops per
+// instruction, so decoding and fetching the stream dominate; this executor has one short path
+// per opcode and no block-shape dispatch.
+template <typename T>
+__device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, double *R) {
+  switch (I.op) {
+    case OP_LOADP:
+      A[I.dst] = (T)I.c * A[I.a];
+      break;
+    case OP_LOADC:
+      A[I.dst] = (T)I.c * __ldg(O + I.a);
+      break;
+    case OP_PMUL:
+    case OP_PMULD:
+      A[I.dst] = A[I.a] * A[I.src];
+      break;
+    case OP_OMUL: {  // the roundings of omul_m<T, 1, 1, 1, MODE>
+      const T o = __ldg(O + I.a), x = A[I.src];
+      if (I.w < 0 && I.c == 1.0) {
+        A[I.dst] = I.acc ? fmaT<T>(o, x, A[I.dst]) : o * x;
+      } else {
+        const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
+        const T p = o * x;
+        A[I.dst] = I.acc ? fmaT<T>(coef, p, A[I.dst]) : coef * p;
+      }
+      break;
+    }
+    case OP_AXPY: {  // the roundings of axpy_u<T, 1>
+      const T x = A[I.src];
+      if (I.w < 0 && I.c == 1.0) {
+        A[I.dst] = I.acc ? x + A[I.dst] : x;
+      } else {
+        const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
+        A[I.dst] = I.acc ? fmaT<T>(coef, x, A[I.dst]) : coef * x;
+      }
+      break;
+    }
+    case OP_LEAF:
+      R[I.a] += (double)A[I.src];
+      break;
+    default:
+      break;
+  }
+}
+
+template <typename T, int RESMAX>
+__device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, double *R) {
+  const int rows = I.rows, cols = I.cols;
+  switch (I.op) {
+    case OP_LOADP: {
+      const T c = (T)I.c;
+      if (I.inner) {
+#pragma unroll 1
+        for (int j = 0; j < rows; ++j)
+#pragma unroll 1
+          for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = (r == j) ? c * A[I.a + r] : (T)0;
+      } else {
+#pragma unroll 1
+        for (int e = 0; e < rows * rows; ++e) A[I.dst + e] = c * A[I.a + e];
+      }
+      break;
+    }
+    case OP_LOADC: {
+      const T c = (T)I.c;
+#pragma unroll 1
+      for (int e = 0; e < rows * cols; ++e) A[I.dst + e] = c * __ldg(O + I.a + e);
+      break;
+    }
+    case OP_PMUL: {
+      const int cr = dcode(rows), cc = dcode(cols);
+      if (cr >= 0 && cc >= 0) {
+        const int code = cr * 3 + cc;
+        QIW_D2(pmul_u, A, I.dst, I.a, I.src)
+      } else {
+#pragma unroll 1
+        for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+          for (int r = 0; r < rows; ++r) {
+            T acc = (T)0;
+#pragma unroll 4
+            for (int k = 0; k < rows; ++k) acc = fmaT<T>(A[I.a + k * rows + r], A[I.src + j * rows + k], acc);
+            A[I.dst + j * rows + r] = acc;
+          }
+      }
+      break;
+    }
+    case OP_PMULD: {
+      const int cr = dcode(rows), cc = dcode(cols);
+      if (cr >= 0 && cc >= 0) {
+        const int code = cr * 3 + cc;
+        QIW_D2(pmuld_u, A, I.dst, I.a, I.src)
+      } else {
+#pragma unroll 1
+        for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+          for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = A[I.a + r] * A[I.src + j * rows + r];
+      }
+      break;
+    }
+    case OP_OMUL: {
+      const int inner = I.inner;
+      const bool has_coef = (I.w >= 0) || (I.c != 1.0);
+      const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
+      const int cr = dcode(rows), ck = dcode(inner), cc = dcode(cols);
+      if (cr >= 0 && ck >= 0 && cc >= 0) {
+        const int code = cr * 9 + ck * 3 + cc;
+        QIW_D3(omul_u, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef)
+      } else {
+#pragma unroll 1
+        for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+          for (int r = 0; r < rows; ++r) {
+            T acc = (T)0;
+#pragma unroll 4
+            for (int k = 0; k < inner; ++k) acc = fmaT<T>(__ldg(O + I.a + k * rows + r), A[I.src + j * inner + k], acc);
+            const int o = I.dst + j * rows + r;
+            A[o] = I.acc ? fmaT<T>(coef, acc, A[o]) : coef * acc;
+          }
+      }
+      break;
+    }
+    case OP_AXPY: {
+      const bool has_coef = (I.w >= 0) || (I.c != 1.0);
+      const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
+      const int n = rows * cols;
+      const bool accf = I.acc != 0;
+      switch (n) {
+        case 1: axpy_u<T, 1>(A, I.dst, I.src, coef, accf, has_coef); break;
+        case 2: axpy_u<T, 2>(A, I.dst, I.src, coef, accf, has_coef); break;
+        case 4: axpy_u<T, 4>(A, I.dst, I.src, coef, accf, has_coef); break;
+        case 8: axpy_u<T, 8>(A, I.dst, I.src, coef, accf, has_coef); break;
+        case 16: axpy_u<T, 16>(A, I.dst, I.src, coef, accf, has_coef); break;
+        default:
+#pragma unroll 1
+          for (int e = 0; e < n; ++e) {
+            const int o = I.dst + e;
+            A[o] = accf ? fmaT<T>(coef, A[I.src + e], A[o]) : coef * A[I.src + e];
+          }
+      }
+      break;
+    }
+    case OP_LEAF: {
+#pragma unroll 1
+      for (int e = 0; e < rows * cols; ++e) R[I.a + e] += (double)A[I.src + e];
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Times and sample range of one tile: t_i, t_w, t_f of the work item, the Sobol index of its
+// first sample (first_index), the work item's sample count, the Sobol tables and the optional
+// warped points / per-sample output of qiw_integrate_warped / qiw_integrate_samples.  The
+// single-problem kernel passes its DevWork (same field names) straight from global memory.
+struct TileSrc {
+  double t_i, t_w, t_f;
+  uint64_t first_index, n_samples;
+  const uint32_t *m, *x0;
+  const double *pts;
+  double *sample_out;
+};
+
+// One tile: blockDim.x samples [s0, s0 + blockDim.x) of batch `batch` of group g, reduced to
+// the CTA's partial sums at partial_row()[0 .. res_size).  Every thread of the CTA must call it.
+// EXTRAS compiles in the warped points and the per-sample output (qiw_integrate_warped /
+// qiw_integrate_samples); the plain kernels are built without them (fewer live registers).
+template <typename T, int ARENA, int RESMAX, bool EXTRAS, typename Src, typename RowFn>
+__device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &g, const Src &w, int batch,
+                                          uint64_t s0, RowFn partial_row) {
+  const uint64_t sidx = s0 + threadIdx.x;
+  const bool active = sidx < w.n_samples;
+  const int res_size = g.res_size;
+
+  T A[ARENA];
+  double R[RESMAX];
+#pragma unroll 1
+  for (int e = 0; e < res_size; ++e) R[e] = 0.0;
+
+  double wt = 1.0;
+  if (active) {
+    double tm[kMaxNodes];
+    const double tsel[3] = {w.t_i, w.t_w, w.t_f};
+#pragma unroll 1
+    for (int f = 0; f < g.n_fixed; ++f) tm[g.fixed_pos[f]] = tsel[g.fixed_time[f]];
+    const int D = g.D;
+    if (D > 0) {
+      const uint64_t n = w.first_index + sidx;
+      const uint32_t gray = (uint32_t)(n ^ (n >> 1));
+      double u[kMaxDim];
+#pragma unroll 1
+      if (EXTRAS && w.pts) {  // warped point x = w(y) of a learned change of variables, weight 1/q(x)
+        const double *pp = w.pts + sidx * (uint64_t)(D + 1);
+#pragma unroll 1
+        for (int d = 0; d < D; ++d) u[d] = pp[d];
+        wt = pp[D];
+      } else {
+#pragma unroll 1
+        for (int d = 0; d < D; ++d) {
+          uint32_t v = __ldg(w.x0 + d);
+          const uint32_t *md = w.m + d * 32;
+#pragma unroll 8
+          for (int b = 0; b < 32; ++b)
+            if ((gray >> b) & 1u) v ^= __ldg(md + b);
+          u[d] = ldexp((double)v, -32);  // exact: ldexp(Float64(x), -32)
+        }
+      }
+      if (g.kind == 1) {  // RootTransform over [t_i, t_f]
+        const double u_diff = w.t_f - w.t_i;
+        double acc = pow(u[0], 1.0 / (double)D);
+        u[0] = acc;
+#pragma unroll 1
+        for (int i = 2; i <= D; ++i) {
+          acc = acc * pow(u[i - 1], 1.0 / (double)(D - i + 1));
+          u[i - 1] = acc;
+        }
+#pragma unroll 1
+        for (int i = 0; i < D; ++i) u[i] = w.t_i + u[i] * u_diff;
+      } else {  // DoubleSimplexRootTransform
+        const int dg = g.d_after, dl = g.d_before;
+        const double fw = w.t_f - w.t_w, wi = w.t_w - w.t_i;
+        double acc = pow(u[0], 1.0 / (double)dg);
+        u[0] = acc;
+#pragma unroll 1
+        for (int i = 2; i <= dg; ++i) {
+          acc = acc * pow(u[i - 1], 1.0 / (double)(dg - i + 1));
+          u[i - 1] = acc;
+        }
+#pragma unroll 1
+        for (int i = 0; i < dg; ++i) u[i] = u[i] * fw + w.t_w;
+        if (dl > 0) {
+          acc = pow(u[dg], 1.0 / (double)dl);
+          u[dg] = acc;
+#pragma unroll 1
+          for (int i = dg + 2; i <= D; ++i) {
+            acc = acc * pow(u[i - 1], 1.0 / (double)(D - i + 1));
+            u[i - 1] = acc;
+          }
+#pragma unroll 1
+          for (int i = dg; i < D; ++i) u[i] = u[i] * wi + w.t_i;
+        }
+      }
+#pragma unroll 1
+      for (int j = 0; j < D; ++j) tm[g.var_pos[j]] = u[j];
+    }
+
+    // i*P blocks of the intervals the program uses.
+    const T *Ptab = reinterpret_cast<const T *>(pb.P);
+#pragma unroll 1
+    for (int j = 0; j < g.n_pm; ++j) {
+      const PmJob job = g.pm[j];
+      double dt = tm[job.iv + 1] - tm[job.iv];
+      dt = dt < 0.0 ? 0.0 : dt;  // time-ordering violations from rounding (topology_eval.jl:361-364)
+      const int d = pb.dims[job.s];
+      if (g.use_bold) {
+        int i;
+        double f;
+        lin_index(dt, pb.inv_h, pb.n_tau, &i, &f);
+        const T *a = Ptab + pb.ptab_off[job.s] + (size_t)i * d * d;
+        const T ff = (T)f;
+#pragma unroll 1
+        for (int e = 0; e < d * d; ++e) {
+          const T lo = __ldg(a + e), hi = __ldg(a + d * d + e);
+          A[job.off + e] = fmaT<T>(ff, hi - lo, lo);
+        }
+      } else {
+        const double *E = pb.E + pb.eoff[job.s];
+#pragma unroll 1
+        for (int e = 0; e < d; ++e) A[job.off + e] = (T)exp(-dt * __ldg(E + e));
+      }
+    }
+    // i*Delta weights.
+    const T *Dtab = reinterpret_cast<const T *>(pb.delta);
+#pragma unroll 1
+    for (int j = 0; j < g.n_w; ++j) {
+      const WJob job = g.wj[j];
+      double dt = tm[job.tail] - tm[job.head];
+      dt = dt < 0.0 ? 0.0 : dt;  // topology_eval.jl:407-410
+      int i;
+      double f;
+      lin_index(dt, pb.inv_h, pb.n_tau, &i, &f);
+      const T *t = Dtab + pb.delta_off[job.pair];
+      T val;
+      if (pb.delta_kind[job.pair] == 0) {
+        const T lo = __ldg(t + i), hi = __ldg(t + i + 1);
+        val = fmaT<T>((T)f, hi - lo, lo);
+      } else {  // natural cubic spline, per-segment polynomial in f
+        const T *c = t + 4 * i;
+        const T ff = (T)f;
+        val = fmaT<T>(ff, fmaT<T>(ff, fmaT<T>(ff, __ldg(c + 3), __ldg(c + 2)), __ldg(c + 1)), __ldg(c));
+      }
+      A[job.off] = val;
+    }
+
+  }
+
+  // The group's program: the instructions of this CTA's batch.  Scalar programs (all blocks
+  // 1x1) stream them through shared memory in chunks of blockDim.x: each thread copies one
+  // 32-byte instruction of the next chunk with cp.async while the current chunk executes (the
+  // streams are MBs, far beyond L1, and every thread reads every instruction); the waits are
+  // cp.async.wait_group and CTA barriers.  Other programs spend thousands of cycles per
+  // instruction and read them directly.
+  {
+    const T *O = reinterpret_cast<const T *>(pb.opv);
+    const int i0 = __ldg(g.batch_begin + batch), i1 = __ldg(g.batch_begin + batch + 1);
+    if (g.scalar) {  // the launch provides the staging buffers for every scalar group
+      const int ch = blockDim.x;
+      Instr *const ibuf = reinterpret_cast<Instr *>(qiw_dyn_smem + (size_t)((blockDim.x + 31) >> 5) * RESMAX * sizeof(double));
+      stage_instr(ibuf, g.ins, i0, i1);
+      cp_async_commit();
+      int b = 0;
+#pragma unroll 1
+      for (int base = i0; base < i1; base += ch, b ^= 1) {
+        if (base + ch < i1) stage_instr(ibuf + (b ^ 1) * ch, g.ins, base + ch, i1);
+        cp_async_commit();
+        cp_async_wait_1();   // this thread's copies of the current chunk have landed
+        __syncthreads();     // and everyone's
+        const int n = min(ch, i1 - base);
+        if (active) {
+#pragma unroll 1
+          for (int k = 0; k < n; ++k) {
+            const Instr I = ibuf[b * ch + k];
+            exec_scalar<T>(I, A, O, R);
+          }
+        }
+        __syncthreads();     // the buffer is refilled two chunks later
+      }
+      cp_async_wait_0();
+    } else if (active) {
+#pragma unroll 1
+      for (int ip = i0; ip < i1; ++ip) {
+        const Instr I = load_instr(g.ins + ip);
+        exec_instr<T, RESMAX>(I, A, O, R);
+      }
+    }
+  }
+  if (active) {
+    if (EXTRAS && w.pts) {
+#pragma unroll 1
+      for (int e = 0; e < res_size; ++e) R[e] *= wt;
+    }
+    if (EXTRAS && w.sample_out) {  // per-sample values (batches of one sample add up)
+#pragma unroll 1
+      for (int e = 0; e < res_size; ++e) atomicAdd(w.sample_out + sidx * (uint64_t)res_size + e, R[e]);
+    }
+  }
+
+  // Deterministic CTA reduction of R -> prow[0 .. res_size).
+  double(*red)[RESMAX] = reinterpret_cast<double(*)[RESMAX]>(qiw_dyn_smem);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n_warps = (blockDim.x + 31) >> 5;
+#pragma unroll 1
+  for (int e = 0; e < res_size; ++e) {
+    double v = R[e];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][e] = v;
+  }
+  __syncthreads();
+#pragma unroll 1
+  double *prow = partial_row();  // formed only now: nothing holds it across the tile
+#pragma unroll 1
+  for (int e = threadIdx.x; e < res_size; e += blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < n_warps; ++k) s += red[k][e];
+    prow[e] = s;
+  }
+}
+
+template <typename T, int ARENA, int RESMAX, bool EXTRAS>
+__global__ void __launch_bounds__(kMaxThreads, kMinBlocks)
+    eval_kernel(DevProblem pb, const DevGroup *__restrict__ groups, const DevWork *__restrict__ works,
+                const int4 *__restrict__ cta_map, double *__restrict__ partials) {
+  const int4 cm = cta_map[blockIdx.x];   // (work item, batch, first sample of the tile, -)
+  const DevWork &w = works[cm.x];
+  const DevGroup &g = groups[w.group];
+  eval_tile<T, ARENA, RESMAX, EXTRAS>(pb, g, w, cm.y, (uint64_t)cm.z,
+                              [=]() { return partials + (size_t)blockIdx.x * g.res_size; });
+}
+
+}  // namespace qiw

@@ -61,6 +61,8 @@ struct DevGroup {
   int32_t arena;               // elements of the compute type
   int32_t res_size;            // sum d^2 (result elements)
   int32_t n_batches;           // independent instruction ranges (one per initial sector or split)
+  int32_t scalar;              // 1: every block of the program is 1x1 (scalar executor, staged stream)
+  int32_t pad_g;
   const PmJob *pm;
   const WJob *wj;
   const Instr *ins;

@@ -29,6 +29,8 @@ struct LaunchArgs {
   int64_t arena_max;
   int res_max;
   bool fp32;
+  bool extras;               // a work item has warped points or per-sample output
+  bool stage;                // a group is scalar: shared-memory instruction staging buffers
   cudaStream_t stream;
 };
 
@@ -83,6 +85,7 @@ struct BatchArgs {
   int64_t arena_max;
   int res_max;
   bool fp32;
+  bool stage;                // a plan is scalar: shared-memory instruction staging buffers
   cudaStream_t stream;
 };
 
@@ -94,6 +97,7 @@ int batch_occupancy(const BatchArgs &a, int *blocks_per_sm);
 
 int arena_class(int64_t arena);   // 0 small, 1 large, 2 huge, -1 too large
 cudaError_t launch_eval(const LaunchArgs &a);
+cudaError_t launch_eval_extras(const LaunchArgs &a);   // csrc/qiw_kernels_x.cu
 cudaError_t launch_finish(const FinishArgs &a);
 cudaError_t launch_fma_peak(bool fp32, void *out, int blocks, int threads, int iters, cudaStream_t st);
 
