@@ -276,10 +276,20 @@ int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
     delete g;
     return c->fail(QIW_ERR_MEMORY, "qiw_group_create: per-sample arena above the largest kernel instantiation");
   }
+  // flag bit 0 = (c != 1); the FP32 copy holds c rounded to float in the low 4 bytes of c
+  for (Instr &I : g->plan.ins) I.flags = (I.c != 1.0) ? 1 : 0;
+  std::vector<Instr> ins32(g->plan.ins);
+  for (Instr &I : ins32) {
+    const float f = (float)I.c;
+    uint64_t bits = 0;
+    std::memcpy(&bits, &f, sizeof(f));
+    std::memcpy(&I.c, &bits, sizeof(bits));
+  }
   const Plan &p = g->plan;
   if ((rc = c->cuda(g->pm.upload(p.pm.data(), p.pm.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(g->wj.upload(p.wj.data(), p.wj.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(g->ins.upload(p.ins.data(), p.ins.size(), c->stream), "upload plan")) ||
+      (rc = c->cuda(g->ins32.upload(ins32.data(), ins32.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(g->batch.upload(p.batch_begin.data(), p.batch_begin.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(cudaStreamSynchronize(c->stream), "upload plan"))) {
     delete g;
@@ -312,6 +322,7 @@ int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
   dg.pm = g->pm.p;
   dg.wj = g->wj.p;
   dg.ins = g->ins.p;
+  dg.ins32 = g->ins32.p;
   dg.batch_begin = g->batch.p;
   *out = g;
   return QIW_OK;

@@ -355,6 +355,7 @@ void qiw_batch_destroy(qiw_batch *b) {
     e.rec->pm.release();
     e.rec->wj.release();
     e.rec->ins.release();
+    e.rec->ins32.release();
     e.rec->batch.release();
     delete e.rec;
   }

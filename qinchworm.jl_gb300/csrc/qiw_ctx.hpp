@@ -43,7 +43,7 @@ struct GroupRec {
   Plan plan;
   DevBuf<PmJob> pm;
   DevBuf<WJob> wj;
-  DevBuf<Instr> ins;
+  DevBuf<Instr> ins, ins32;
   DevBuf<int32_t> batch;
   DevGroup dg;
 };
@@ -110,6 +110,7 @@ struct qiw_ctx {
       g->pm.release();
       g->wj.release();
       g->ins.release();
+      g->ins32.release();
       g->batch.release();
       delete g;
     }

@@ -201,6 +201,19 @@ __device__ __forceinline__ void axpy_u(T *A, int dst, int src, T coef, bool accf
     default: F<T, 4, 4>(__VA_ARGS__); break;                                                      \
   }
 
+// Instruction coefficient in the compute type: FP64 programs hold c as a double, FP32 programs
+// (DevGroup::ins32) hold it rounded to float in the low 4 bytes of the same slot, so neither
+// path spends FP64-pipe work (compare or convert) per instruction.  Flag bit 0: c != 1.
+template <typename T>
+__device__ __forceinline__ T coef_c(const Instr &I);
+template <>
+__device__ __forceinline__ double coef_c<double>(const Instr &I) { return I.c; }
+template <>
+__device__ __forceinline__ float coef_c<float>(const Instr &I) {
+  return __int_as_float((int)(unsigned)(__double_as_longlong(I.c) & 0xffffffffull));
+}
+__device__ __forceinline__ bool has_c(const Instr &I) { return (I.flags & 1u) != 0; }
+
 // Programs whose blocks are all 1x1 (single-orbital models): about 1.5 flops per
 // instruction, so decoding and fetching the stream dominate; this executor has one short path
 // per opcode and no block-shape dispatch.
@@ -208,10 +221,10 @@ template <typename T>
 __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, double *R) {
   switch (I.op) {
     case OP_LOADP:
-      A[I.dst] = (T)I.c * A[I.a];
+      A[I.dst] = has_c(I) ? coef_c<T>(I) * A[I.a] : A[I.a];
       break;
     case OP_LOADC:
-      A[I.dst] = (T)I.c * __ldg(O + I.a);
+      A[I.dst] = has_c(I) ? coef_c<T>(I) * __ldg(O + I.a) : __ldg(O + I.a);
       break;
     case OP_PMUL:
     case OP_PMULD:
@@ -219,10 +232,10 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
       break;
     case OP_OMUL: {  // the roundings of omul_m<T, 1, 1, 1, MODE>
       const T o = __ldg(O + I.a), x = A[I.src];
-      if (I.w < 0 && I.c == 1.0) {
+      if (I.w < 0 && !has_c(I)) {
         A[I.dst] = I.acc ? fmaT<T>(o, x, A[I.dst]) : o * x;
       } else {
-        const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
+        const T coef = (I.w >= 0) ? (has_c(I) ? coef_c<T>(I) * A[I.w] : A[I.w]) : coef_c<T>(I);
         const T p = o * x;
         A[I.dst] = I.acc ? fmaT<T>(coef, p, A[I.dst]) : coef * p;
       }
@@ -230,10 +243,10 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
     }
     case OP_AXPY: {  // the roundings of axpy_u<T, 1>
       const T x = A[I.src];
-      if (I.w < 0 && I.c == 1.0) {
+      if (I.w < 0 && !has_c(I)) {
         A[I.dst] = I.acc ? x + A[I.dst] : x;
       } else {
-        const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
+        const T coef = (I.w >= 0) ? (has_c(I) ? coef_c<T>(I) * A[I.w] : A[I.w]) : coef_c<T>(I);
         A[I.dst] = I.acc ? fmaT<T>(coef, x, A[I.dst]) : coef * x;
       }
       break;
@@ -250,23 +263,26 @@ template <typename T, int RESMAX>
 __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, double *R) {
   const int rows = I.rows, cols = I.cols;
   switch (I.op) {
-    case OP_LOADP: {
-      const T c = (T)I.c;
+    case OP_LOADP: {  // c == 1 copies (x * 1 is exact)
+      const T c = coef_c<T>(I);
+      const bool hc = has_c(I);
       if (I.inner) {
 #pragma unroll 1
         for (int j = 0; j < rows; ++j)
 #pragma unroll 1
-          for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = (r == j) ? c * A[I.a + r] : (T)0;
+          for (int r = 0; r < rows; ++r)
+            A[I.dst + j * rows + r] = (r == j) ? (hc ? c * A[I.a + r] : A[I.a + r]) : (T)0;
       } else {
 #pragma unroll 1
-        for (int e = 0; e < rows * rows; ++e) A[I.dst + e] = c * A[I.a + e];
+        for (int e = 0; e < rows * rows; ++e) A[I.dst + e] = hc ? c * A[I.a + e] : A[I.a + e];
       }
       break;
     }
     case OP_LOADC: {
-      const T c = (T)I.c;
+      const T c = coef_c<T>(I);
+      const bool hc = has_c(I);
 #pragma unroll 1
-      for (int e = 0; e < rows * cols; ++e) A[I.dst + e] = c * __ldg(O + I.a + e);
+      for (int e = 0; e < rows * cols; ++e) A[I.dst + e] = hc ? c * __ldg(O + I.a + e) : __ldg(O + I.a + e);
       break;
     }
     case OP_PMUL: {
@@ -302,8 +318,8 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
     }
     case OP_OMUL: {
       const int inner = I.inner;
-      const bool has_coef = (I.w >= 0) || (I.c != 1.0);
-      const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
+      const bool has_coef = (I.w >= 0) || has_c(I);
+      const T coef = (I.w >= 0) ? (has_c(I) ? coef_c<T>(I) * A[I.w] : A[I.w]) : coef_c<T>(I);
       const int cr = dcode(rows), ck = dcode(inner), cc = dcode(cols);
       if (cr >= 0 && ck >= 0 && cc >= 0) {
         const int code = cr * 9 + ck * 3 + cc;
@@ -323,8 +339,8 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
       break;
     }
     case OP_AXPY: {
-      const bool has_coef = (I.w >= 0) || (I.c != 1.0);
-      const T coef = (I.w >= 0) ? (I.c == 1.0 ? A[I.w] : (T)I.c * A[I.w]) : (T)I.c;
+      const bool has_coef = (I.w >= 0) || has_c(I);
+      const T coef = (I.w >= 0) ? (has_c(I) ? coef_c<T>(I) * A[I.w] : A[I.w]) : coef_c<T>(I);
       const int n = rows * cols;
       const bool accf = I.acc != 0;
       switch (n) {
@@ -506,15 +522,16 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
   {
     const T *O = reinterpret_cast<const T *>(pb.opv);
     const int i0 = __ldg(g.batch_begin + batch), i1 = __ldg(g.batch_begin + batch + 1);
+    const Instr *ins = sizeof(T) == 4 ? g.ins32 : g.ins;
     if (g.scalar) {  // the launch provides the staging buffers for every scalar group
       const int ch = blockDim.x;
       Instr *const ibuf = reinterpret_cast<Instr *>(qiw_dyn_smem + (size_t)((blockDim.x + 31) >> 5) * RESMAX * sizeof(double));
-      stage_instr(ibuf, g.ins, i0, i1);
+      stage_instr(ibuf, ins, i0, i1);
       cp_async_commit();
       int b = 0;
 #pragma unroll 1
       for (int base = i0; base < i1; base += ch, b ^= 1) {
-        if (base + ch < i1) stage_instr(ibuf + (b ^ 1) * ch, g.ins, base + ch, i1);
+        if (base + ch < i1) stage_instr(ibuf + (b ^ 1) * ch, ins, base + ch, i1);
         cp_async_commit();
         cp_async_wait_1();   // this thread's copies of the current chunk have landed
         __syncthreads();     // and everyone's
@@ -532,7 +549,7 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
     } else if (active) {
 #pragma unroll 1
       for (int ip = i0; ip < i1; ++ip) {
-        const Instr I = load_instr(g.ins + ip);
+        const Instr I = load_instr(ins + ip);
         exec_instr<T, RESMAX>(I, A, O, R);
       }
     }

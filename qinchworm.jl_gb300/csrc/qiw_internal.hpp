@@ -24,7 +24,8 @@ enum Opcode : uint8_t {
 struct alignas(16) Instr {     // 32 bytes
   uint8_t op, rows, inner, cols;
   uint8_t acc;                 // 1: accumulate into dst, 0: overwrite
-  uint8_t pad0, pad1, pad2;
+  uint8_t flags;               // bit 0: c != 1 (set on upload; the kernels test no doubles)
+  uint8_t pad1, pad2;
   int32_t dst;                 // arena offset (elements)
   int32_t src;                 // arena offset (elements)
   int32_t a;                   // Pm offset (arena) / operator value offset / result offset
@@ -66,6 +67,7 @@ struct DevGroup {
   const PmJob *pm;
   const WJob *wj;
   const Instr *ins;
+  const Instr *ins32;          // the same program with c rounded to float in the low 4 bytes of c
   const int32_t *batch_begin;  // [n_batches + 1]
 };
 
