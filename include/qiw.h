@@ -43,6 +43,7 @@ extern "C" {
 #define QIW_GROUP_BOLD 0       /* IdentityNode(t_i), InchNode(t_w), IdentityNode(t_f); P bold  (:161-165) */
 #define QIW_GROUP_BARE 1       /* IdentityNode(t_i), IdentityNode(t_f); exact atomic P0         (:266-268) */
 #define QIW_GROUP_CORRELATOR 2 /* OperatorNode(B,t_i), OperatorNode(A,t_w), IdentityNode(t_f)  (:846-850) */
+#define QIW_GROUP_SIGMA 3      /* self-energy: PairNode(t_i), PairNode(t_f), 2k-2 vertices between (:560-566) */
 
 /* arithmetic of the chain products */
 #define QIW_PREC_FP64 0        /* plain FP64 throughout */
@@ -118,11 +119,21 @@ typedef struct {
 
 int qiw_group_stats_get(qiw_ctx *ctx, int32_t group_id, qiw_group_stats *out);
 
+/* Domain maps of a bare group (src/qmc_integrate.jl): the default is RootTransform (:198-258);
+ * SortTransform (:282-334) maps x to t_i + sort(x, rev=true) (t_f - t_i); ExpModelFunctionTransform
+ * (:99-165) maps x to u_1 = t_f + tau log(1 - x_1), u_n = u_{n-1} + tau log(1 - x_n) with the
+ * per-sample Jacobian tau^d / exp(-(t_f - u_d) / tau), discarding samples with u_d < 0 as
+ * contour_integral does (:597-612); it needs t_i = 0 and takes tau from t_w.  Bold and correlator
+ * groups take the default (DoubleSimplexRootTransform, :363-463) only. */
+#define QIW_TRANSFORM_DEFAULT 0
+#define QIW_TRANSFORM_SORT 1
+#define QIW_TRANSFORM_EXPMODEL 2
+
 /* One qMC integral of one group over a contiguous Sobol index range. */
 typedef struct {
     int32_t group;
-    int32_t reserved;
-    double t_i, t_w, t_f;              /* t_w unused for QIW_GROUP_BARE */
+    int32_t transform;                 /* QIW_TRANSFORM_* (bare groups), else 0 */
+    double t_i, t_w, t_f;              /* t_w unused for QIW_GROUP_BARE (EXPMODEL: the decay rate) */
     uint64_t first_index;              /* 0-based Sobol point index = first(N_range) - 1 */
     uint64_t n_samples;                /* length(N_range) */
     uint64_t n_total;                  /* td.N_samples (rank_weight = n_samples / n_total) */

@@ -63,7 +63,8 @@ class _Group(C.Structure):
                 ("t_i", C.c_double), ("t_w", C.c_double), ("t_f", C.c_double),
                 ("n_fixed", C.c_int), ("fixed_pos", C.c_void_p), ("fixed_kind", C.c_void_p),
                 ("fixed_op", C.c_void_p), ("fixed_time", C.c_void_p),
-                ("n_top", C.c_int), ("top_pairs", C.c_void_p), ("top_parity", C.c_void_p)]
+                ("n_top", C.c_int), ("top_pairs", C.c_void_p), ("top_parity", C.c_void_p),
+                ("decay", C.c_double)]
 
 
 _lib = None
@@ -282,11 +283,19 @@ class OracleProblem:
 
     def integrate(self, kind: str, order: int, n_pts_after: int, tops, t_i: float, t_w: float,
                   t_f: float, N: int, n_ranks: int = 1, m=None, x0=None, corr: Optional[int] = None,
-                  sample_range=None):
-        """One group: kind 'bold', 'bare' or 'corr'; returns per-sector diagonal blocks."""
+                  sample_range=None, transform: str = "root", decay: float = 0.0):
+        """One group: kind 'bold', 'bare', 'corr' or 'sigma'; returns per-sector diagonal blocks.
+        Bare groups take transform 'root' (default), 'sort' or 'expmodel' (decay rate `decay`)."""
+        n_pair_fixed = 0
         if kind == "bare":
             fixed = [(0, 2, 0, t_i), (2 * order + 1, 2, 0, t_f)]
-            transform, d_before, d_after, use_bold = 0, 0, 0, 0
+            transform, d_before, d_after, use_bold = {"root": 0, "sort": 2, "expmodel": 3}[transform], 0, 0, 0
+        elif kind == "sigma":
+            # self-energy diagrams of diff_inchworm_step! (src/inchworm.jl:560-566): PairNodes
+            # fixed at t_i and t_f, the 2k - 2 other vertices integrated over [t_i, t_f] (Root)
+            fixed = [(0, 1, 0, t_i), (2 * order - 1, 1, 0, t_f)]
+            transform, d_before, d_after, use_bold = 0, 0, 0, 1
+            n_pair_fixed = 2
         else:
             d_after = n_pts_after
             d_before = 2 * order - n_pts_after
@@ -304,8 +313,8 @@ class OracleProblem:
         par = np.array([p for (_, p) in tops] or [1], dtype=np.int32)
         gr = _Group(order, use_bold, transform, d_before, d_after, t_i, t_w, t_f, len(fixed),
                     fp.ctypes.data, fk.ctypes.data, fo.ctypes.data, ft.ctypes.data, len(tops),
-                    tp.ctypes.data, par.ctypes.data)
-        D = 2 * order
+                    tp.ctypes.data, par.ctypes.data, decay)
+        D = 2 * order - n_pair_fixed
         if m is None:
             m = sobol_directions(D) if D > 0 else np.zeros((1, 32), np.uint32)
         m = np.ascontiguousarray(m, dtype=np.uint32)
@@ -360,6 +369,58 @@ def inchworm(exp, orders, orders_bare, N_samples: int, n_pts_after_max: Optional
         pb.set_ppgf(n + 1, total)
         pb.normalize_tau(n + 1)
     return pb
+
+
+def diff_inchworm(exp, orders, N_samples: int, n_ranks: int = 1, conv_factor: complex = -1j):
+    """diff_inchworm! restated (src/inchworm.jl:529-786); returns (OracleProblem, Sigma tables).
+
+    Per step n (tau_f_prev = tau_n, tau_f = tau_{n+1}): Sigma(tau_n) = sum over orders k >= 1 of
+    the self-energy diagrams (topologies with n_pts_after = 1, PairNodes at tau_0 and tau_n);
+    conv = integral over [tau_0, tau_n] of Sigma(tau_n - tau) P(tau), trapezoid rule on the grid
+    (Keldysh's integrate; its contour measure on the imaginary branch is `conv_factor` * h);
+    P(tau_{n+1}) = P(tau_n) + h (conv - H P(tau_n)) with H_s = diag(E_s + lambda) (Euler,
+    Delta tau = 1im * step = h).  No normalisation.  With spline-interpolated P the stored
+    Sigma lags one grid point, as the reference's incremental-spline container does."""
+    pb = OracleProblem(exp)
+    grid = exp.grid
+    S = pb.S
+    h = grid.step
+    groups = []
+    for order in orders:
+        if order == 0:
+            continue
+        tops = topologies(order, 1)
+        if tops:
+            groups.append((order, tops))
+    H = [np.diag(P0.E).astype(np.complex128) for P0 in exp.P0]
+    sigma = [np.zeros_like(d) for d in pb.P_data]
+    for n in range(0, grid.n_tau - 1):
+        t_i, t_prev = grid.tau(0), grid.tau(n)
+        P_prev = [pb.P_data[s][n].copy() for s in range(S)]
+        total = [np.zeros((d, d), np.complex128) for d in pb.dims]
+        for (order, tops) in groups:
+            blk = pb.integrate("sigma", order, 1, tops, t_i, 0.0, t_prev, N_samples, n_ranks)
+            total = [a + b for a, b in zip(total, blk)]
+        # set_ppgf!(Sigma, tau_i, tau_n, .): with spline-interpolated P, Sigma = zero(P) is an
+        # incremental spline whose interpolant already holds the tau_0 point, so extend! stores
+        # the value one grid point later (src/ppgf.jl:474-482, src/spline_gf.jl:333-336, 377-386)
+        j_store = n + 1 if pb.spline_P else n
+        if j_store < grid.n_tau:
+            for s in range(S):
+                sigma[s][j_store] = total[s]
+        new = []
+        for s in range(S):
+            conv = np.zeros_like(P_prev[s])
+            for j in range(0, n + 1):
+                w = 0.5 if (j == 0 or j == n) else 1.0
+                if n == 0:
+                    w = 0.0
+                conv = conv + w * (sigma[s][n - j] @ pb.P_data[s][j])
+            conv = conv_factor * h * conv
+            rhs = conv - H[s] @ P_prev[s]
+            new.append(P_prev[s] + h * rhs)
+        pb.set_ppgf(n + 1, new)
+    return pb, sigma
 
 
 def correlator_2p(pb: OracleProblem, orders, N_samples: int, n_ranks: int = 1,

@@ -5,6 +5,7 @@
  * algorithm for one qMC integral of one topology group:
  *   - Sobol direction numbers and next!/skip!     src/scrambled_sobol.jl:66-208
  *   - Root / DoubleSimplexRoot transforms, J      src/qmc_integrate.jl:46,198-258,363-463
+ *   - Sort / ExpModelFunction transforms          src/qmc_integrate.jl:99-165,282-334
  *   - contour_integral / qmc_integral             src/qmc_integrate.jl:497-507,565-612
  *   - TopologyEvaluator ctor + per-sample functor src/topology_eval.jl:249-437
  *   - _traverse_configuration_tree!               src/topology_eval.jl:454-556
@@ -136,6 +137,22 @@ static void root_map(int d, double u_i, double u_diff, const double *x, double *
     for (int i = 0; i < d; ++i) u[i] = u_i + u[i] * u_diff;
 }
 
+/* src/qmc_integrate.jl:319-321 (SortTransform): u = u_i .+ sort(x, rev=true) * u_diff */
+static void sort_map(int d, double u_i, double u_diff, const double *x, double *u)
+{
+    for (int i = 0; i < d; ++i) u[i] = x[i];
+    for (int i = 1; i < d; ++i)            /* insertion sort, descending */
+        for (int j = i; j > 0 && u[j] > u[j - 1]; --j) { double t = u[j]; u[j] = u[j - 1]; u[j - 1] = t; }
+    for (int i = 0; i < d; ++i) u[i] = u_i + u[i] * u_diff;
+}
+
+/* src/qmc_integrate.jl:138-147 (ExpModelFunctionTransform) */
+static void expmodel_map(int d, double u_f, double tau, const double *x, double *u)
+{
+    u[0] = u_f + tau * log(1 - x[0]);
+    for (int i = 1; i < d; ++i) u[i] = u[i - 1] + tau * log(1 - x[i]);
+}
+
 /* src/qmc_integrate.jl:425-449 (DoubleSimplexRootTransform) */
 static void dsimplex_map(int d_lesser, int d_greater, double u_i, double u_w, double diff_wi,
                          double diff_fw, const double *x, double *u)
@@ -234,6 +251,7 @@ typedef struct {
     double times[MAXN];
     int top_to_conf[MAXN];
     int var_pos[MAXN];
+    int n_var;                  /* integrated times: 2k minus the fixed pair vertices */
     /* ppgf_mats[i][s]: i*P(t_{i+1}, t_i) */
     cplx *pm;           /* [(n-1)][S] blocks of MAXD*MAXD */
     /* finite-time node matrices: [pos][opslot][s] blocks; op slots: 2*n_pairs (+1 fixed) */
@@ -364,6 +382,15 @@ static int traverse(evalctx *e, int pos, int s_i, int s_f, cplx w)
     return rc;
 }
 
+/* Integrated times of a group: 2k minus the fixed pair vertices (PairNode, used by the
+   self-energy diagrams of diff_inchworm!, src/inchworm.jl:560-566). */
+static int group_D(const qiwo_group *gr)
+{
+    int D = 2 * gr->order;
+    for (int f = 0; f < gr->n_fixed; ++f) D -= gr->fixed_kind[f] == NK_PAIR;
+    return D;
+}
+
 /* Builds the conf skeleton (fixed nodes) and position maps (topology_eval.jl:254-275). */
 static int setup(evalctx *e, const qiwo_problem *pb, const qiwo_group *gr)
 {
@@ -389,6 +416,7 @@ static int setup(evalctx *e, const qiwo_problem *pb, const qiwo_group *gr)
         if (is_fixed[pos] != 2) e->top_to_conf[k++] = pos;
         if (!is_fixed[pos]) e->var_pos[v++] = pos;
     }
+    e->n_var = v;
     int S = pb->n_sectors;
     e->nm_nops = 2 * pb->n_pairs;
     e->pm = calloc((size_t)(e->n > 1 ? e->n - 1 : 1) * S * BLK, sizeof(cplx));
@@ -416,7 +444,7 @@ static int evaluate(evalctx *e, const double *var_times)
     const qiwo_group *gr = e->gr;
     int S = pb->n_sectors, n = e->n;
     for (int f = 0; f < gr->n_fixed; ++f) e->times[gr->fixed_pos[f]] = gr->fixed_time[f];
-    for (int j = 0; j < 2 * gr->order; ++j) e->times[e->var_pos[j]] = var_times[j];
+    for (int j = 0; j < e->n_var; ++j) e->times[e->var_pos[j]] = var_times[j];
 
     for (int i = 0; i < n - 1; ++i) {
         double ti = e->times[i], tf = e->times[i + 1];
@@ -503,10 +531,10 @@ static void *run_range(void *arg)
     evalctx e;
     jb->rc = setup(&e, pb, gr);
     if (jb->rc) { teardown(&e); return NULL; }
-    int D = 2 * gr->order;
+    int D = group_D(gr);
     for (int s = 0; s < S; ++s) memset(jb->out + (size_t)s * BLK, 0, sizeof(cplx) * BLK);
 
-    if (gr->order == 0) {
+    if (D == 0) {   /* nothing to integrate: one exact evaluation (order 0, order-1 self-energy) */
         jb->rc = evaluate(&e, NULL);
         if (!jb->rc)
             for (int s = 0; s < S; ++s) memcpy(jb->out + (size_t)s * BLK, e.result + (size_t)s * BLK, sizeof(cplx) * BLK);
@@ -515,8 +543,11 @@ static void *run_range(void *arg)
     }
 
     double J;
-    if (gr->transform == QIWO_ROOT) J = simplex_volume(D, gr->t_f - gr->t_i);
+    if (gr->transform == QIWO_ROOT || gr->transform == QIWO_SORT) J = simplex_volume(D, gr->t_f - gr->t_i);
+    else if (gr->transform == QIWO_EXPMODEL) J = 0.0;   /* per sample, below */
     else J = simplex_volume(gr->d_before, gr->t_w - gr->t_i) * simplex_volume(gr->d_after, gr->t_f - gr->t_w);
+    /* src/qmc_integrate.jl:158-164: tau^d / exp(-(u_f - u_d) / tau) */
+    const double exp_norm = gr->transform == QIWO_EXPMODEL ? pow(gr->decay, (double)D) : 0.0;
     /* prod(branch_direction) over 2k imaginary-branch points: (-i)^(2k) */
     cplx bdir = 1.0;
     for (int j = 0; j < D; ++j) bdir *= -I;
@@ -528,10 +559,13 @@ static void *run_range(void *arg)
     for (int64_t i = 0; i < jb->count; ++i) {
         sobol_next(&sq, x);
         if (gr->transform == QIWO_ROOT) root_map(D, gr->t_i, gr->t_f - gr->t_i, x, u);
+        else if (gr->transform == QIWO_SORT) sort_map(D, gr->t_i, gr->t_f - gr->t_i, x, u);
+        else if (gr->transform == QIWO_EXPMODEL) expmodel_map(D, gr->t_f, gr->decay, x, u);
         else dsimplex_map(gr->d_before, gr->d_after, gr->t_i, gr->t_w, gr->t_w - gr->t_i, gr->t_f - gr->t_w, x, u);
         int neg = 0;
         for (int j = 0; j < D; ++j) if (u[j] < 0.0) neg = 1;
         if (neg) continue;
+        if (gr->transform == QIWO_EXPMODEL) J = exp_norm / exp(-(gr->t_f - u[D - 1]) / gr->decay);
         jb->rc = evaluate(&e, u);
         if (jb->rc) break;
         for (int s = 0; s < S; ++s) {
@@ -556,11 +590,12 @@ int qiwo_integrate(const qiwo_problem *pb, const qiwo_group *gr, const uint32_t 
 {
     int S = pb->n_sectors;
     if (n_ranks < 1) n_ranks = 1;
-    if (gr->order == 0) n_ranks = 1;
+    const int exact = group_D(gr) == 0;
+    if (exact) n_ranks = 1;
     job_t *jobs = calloc(n_ranks, sizeof(job_t));
     pthread_t *th = calloc(n_ranks, sizeof(pthread_t));
     cplx *bufs = calloc((size_t)n_ranks * S * BLK, sizeof(cplx));
-    int64_t q = gr->order == 0 ? 1 : N / n_ranks, r = gr->order == 0 ? 0 : N % n_ranks, start = 0;
+    int64_t q = exact ? 1 : N / n_ranks, r = exact ? 0 : N % n_ranks, start = 0;
     for (int k = 0; k < n_ranks; ++k) {
         int64_t cnt = q + (k < r ? 1 : 0);
         jobs[k] = (job_t){pb, gr, m, x0, start, cnt, N, bufs + (size_t)k * S * BLK, 0};
@@ -600,7 +635,8 @@ int qiwo_integrate_range(const qiwo_problem *pb, const qiwo_group *gr, const uin
 {
     int S = pb->n_sectors;
     cplx *buf = calloc((size_t)S * BLK, sizeof(cplx));
-    job_t jb = (job_t){pb, gr, m, x0, first, gr->order == 0 ? 1 : count, gr->order == 0 ? 1 : N_total, buf, 0};
+    const int exact = group_D(gr) == 0;
+    job_t jb = (job_t){pb, gr, m, x0, first, exact ? 1 : count, exact ? 1 : N_total, buf, 0};
     if (jb.count > 0) run_range(&jb);
     size_t off = 0;
     for (int s = 0; s < S; ++s) {

@@ -14,7 +14,7 @@
 #define QIWO_ERR_OFFDIAG 2
 
 enum { QIWO_INTERP_LINEAR = 0, QIWO_INTERP_CUBIC = 1 };
-enum { QIWO_ROOT = 0, QIWO_DSIMPLEX = 1 };
+enum { QIWO_ROOT = 0, QIWO_DSIMPLEX = 1, QIWO_SORT = 2, QIWO_EXPMODEL = 3 };
 
 typedef struct {
     int kind;          /* QIWO_INTERP_LINEAR or QIWO_INTERP_CUBIC */
@@ -52,7 +52,7 @@ typedef struct {
 typedef struct {
     int order;
     int use_bold;
-    int transform;     /* QIWO_ROOT (bare) or QIWO_DSIMPLEX (bold, correlator) */
+    int transform;     /* QIWO_ROOT, QIWO_SORT or QIWO_EXPMODEL (bare), QIWO_DSIMPLEX (bold, correlator) */
     int d_before, d_after;
     double t_i, t_w, t_f;
     int n_fixed;
@@ -63,6 +63,7 @@ typedef struct {
     int n_top;
     const int32_t *top_pairs;    /* [n_top][order][2], 1-based topology vertices */
     const int32_t *top_parity;   /* [n_top] */
+    double decay;                /* QIWO_EXPMODEL: decay rate tau of the model function */
 } qiwo_group;
 
 int qiwo_sobol_directions(int D, const int64_t *poly, const int64_t *vinit, int vinit_cols, uint32_t *m);

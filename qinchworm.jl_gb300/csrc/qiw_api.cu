@@ -145,7 +145,8 @@ int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
     const Plan &p = c->groups[wd.group]->plan;
     if (p.use_bold) need_P = true;
     if (p.D > 0 && (!wd.sobol_m || !wd.sobol_x0)) return c->fail(QIW_ERR_ARG, "qiw_integrate: Sobol tables missing");
-    if (!(wd.t_i <= wd.t_f) || (p.kind != QIW_GROUP_BARE && !(wd.t_i <= wd.t_w && wd.t_w <= wd.t_f)))
+    const bool no_tw = p.kind == QIW_GROUP_BARE || p.kind == QIW_GROUP_SIGMA;
+    if (!(wd.t_i <= wd.t_f) || (!no_tw && !(wd.t_i <= wd.t_w && wd.t_w <= wd.t_f)))
       return c->fail(QIW_ERR_ARG, "qiw_integrate: times must satisfy t_i <= t_w <= t_f");
     if (p.D > 0 && (wd.n_total == 0 || wd.first_index + wd.n_samples > (1ull << 32)))
       return c->fail(QIW_ERR_ARG, "qiw_integrate: Sobol index range beyond 2^32 or N_total = 0");
@@ -156,15 +157,31 @@ int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
     w.t_w = wd.t_w;
     w.t_f = wd.t_f;
     w.first_index = wd.first_index;
+    if (wd.transform != QIW_TRANSFORM_DEFAULT) {
+      if (wd.transform != QIW_TRANSFORM_SORT && wd.transform != QIW_TRANSFORM_EXPMODEL)
+        return c->fail(QIW_ERR_ARG, "qiw_integrate: unknown transform");
+      if (p.kind != QIW_GROUP_BARE) return c->fail(QIW_ERR_ARG, "qiw_integrate: SORT / EXPMODEL maps apply to bare groups");
+      if (wd.transform == QIW_TRANSFORM_EXPMODEL && (wd.t_i != 0.0 || !(wd.t_w > 0.0)))
+        return c->fail(QIW_ERR_ARG, "qiw_integrate: EXPMODEL needs t_i = 0 and the decay rate (t_w) > 0");
+      w.transform = wd.transform;
+      w.decay = wd.t_w;
+    }
+    // Phase of the result: the kernels compute real chains and the finish step returns
+    // -i * scale * sum.  Bold, bare and correlator groups carry -i * parity (the reference's
+    // -i parity (-1)^k times (-i)^(2k) branch factors); self-energy groups integrate 2k - 2
+    // times only, which leaves +i * parity: their scale is negated.
+    const double phase = (p.kind == QIW_GROUP_SIGMA) ? -1.0 : 1.0;
     if (p.D == 0) {
       w.n_samples = 1;
-      w.scale = 1.0;  // order 0: evaluated exactly, no qMC average
+      w.scale = phase;  // order 0 (and order-1 self-energy): evaluated exactly, no qMC average
+      w.transform = QIW_TRANSFORM_DEFAULT;
     } else {
       w.n_samples = wd.n_samples;
-      double J = (p.kind == QIW_GROUP_BARE)
+      double J = (p.kind == QIW_GROUP_BARE || p.kind == QIW_GROUP_SIGMA)
                      ? simplex_volume(p.D, wd.t_f - wd.t_i)
                      : simplex_volume(p.d_before, wd.t_w - wd.t_i) * simplex_volume(p.d_after, wd.t_f - wd.t_w);
-      w.scale = J / (double)wd.n_total;
+      if (w.transform == QIW_TRANSFORM_EXPMODEL) J = 1.0;  // per sample in the kernel
+      w.scale = phase * J / (double)wd.n_total;
     }
     const int n_tiles = (int)((w.n_samples + threads - 1) / threads);
     const int n_b = std::max(0, (int)p.batch_begin.size() - 1);
@@ -226,7 +243,7 @@ int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const De
   la.extras = false;
   la.stage = false;
   for (const DevWork &w : t.works) {
-    la.extras = la.extras || w.pts != nullptr || w.sample_out != nullptr;
+    la.extras = la.extras || w.pts != nullptr || w.sample_out != nullptr || w.transform != QIW_TRANSFORM_DEFAULT;
     la.stage = la.stage || c->groups[w.group]->dg.scalar != 0;
   }
   la.stream = c->stream;

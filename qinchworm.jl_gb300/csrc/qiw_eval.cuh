@@ -226,6 +226,9 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
     case OP_LOADC:
       A[I.dst] = has_c(I) ? coef_c<T>(I) * __ldg(O + I.a) : __ldg(O + I.a);
       break;
+    case OP_LOADI:
+      A[I.dst] = coef_c<T>(I);
+      break;
     case OP_PMUL:
     case OP_PMULD:
       A[I.dst] = A[I.a] * A[I.src];
@@ -276,6 +279,14 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
 #pragma unroll 1
         for (int e = 0; e < rows * rows; ++e) A[I.dst + e] = hc ? c * A[I.a + e] : A[I.a + e];
       }
+      break;
+    }
+    case OP_LOADI: {  // c * identity
+      const T c = coef_c<T>(I);
+#pragma unroll 1
+      for (int j = 0; j < rows; ++j)
+#pragma unroll 1
+        for (int r = 0; r < rows; ++r) A[I.dst + j * rows + r] = (r == j) ? c : (T)0;
       break;
     }
     case OP_LOADC: {
@@ -388,7 +399,7 @@ template <typename T, int ARENA, int RESMAX, bool EXTRAS, typename Src, typename
 __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &g, const Src &w, int batch,
                                           uint64_t s0, RowFn partial_row) {
   const uint64_t sidx = s0 + threadIdx.x;
-  const bool active = sidx < w.n_samples;
+  bool active = sidx < w.n_samples;   // cleared for samples a domain map discards
   const int res_size = g.res_size;
 
   T A[ARENA];
@@ -424,7 +435,35 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
           u[d] = ldexp((double)v, -32);  // exact: ldexp(Float64(x), -32)
         }
       }
-      if (g.kind == 1) {  // RootTransform over [t_i, t_f]
+      bool mapped = false;  // the alternative maps of bare groups live in the extras kernel
+      if constexpr (EXTRAS) {
+        if (g.kind == QIW_GROUP_BARE && w.transform == QIW_TRANSFORM_SORT) {  // SortTransform (src/qmc_integrate.jl:319-321)
+          const double u_diff = w.t_f - w.t_i;
+#pragma unroll 1
+          for (int i = 1; i < D; ++i)  // insertion sort, descending
+#pragma unroll 1
+            for (int j = i; j > 0 && u[j] > u[j - 1]; --j) {
+              const double t = u[j];
+              u[j] = u[j - 1];
+              u[j - 1] = t;
+            }
+#pragma unroll 1
+          for (int i = 0; i < D; ++i) u[i] = w.t_i + u[i] * u_diff;
+          mapped = true;
+        } else if (g.kind == QIW_GROUP_BARE && w.transform == QIW_TRANSFORM_EXPMODEL) {
+          // ExpModelFunctionTransform (src/qmc_integrate.jl:138-164): per-sample Jacobian
+          // tau^d / exp(-(u_f - u_d) / tau); samples below the contour start are discarded
+          const double tau = w.decay;
+          u[0] = w.t_f + tau * log(1.0 - u[0]);
+#pragma unroll 1
+          for (int i = 1; i < D; ++i) u[i] = u[i - 1] + tau * log(1.0 - u[i]);
+          if (u[D - 1] < 0.0) active = false;
+          wt *= pow(tau, (double)D) / exp(-(w.t_f - u[D - 1]) / tau);
+          mapped = true;
+        }
+      }
+      if (mapped) {
+      } else if (g.kind == QIW_GROUP_BARE || g.kind == QIW_GROUP_SIGMA) {  // RootTransform over [t_i, t_f]
         const double u_diff = w.t_f - w.t_i;
         double acc = pow(u[0], 1.0 / (double)D);
         u[0] = acc;
@@ -555,7 +594,7 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
     }
   }
   if (active) {
-    if (EXTRAS && w.pts) {
+    if (EXTRAS && wt != 1.0) {  // warp weight 1/q(x) and / or the ExpModel Jacobian
 #pragma unroll 1
       for (int e = 0; e < res_size; ++e) R[e] *= wt;
     }

@@ -7,7 +7,7 @@ namespace qiw {
 // Limits of the device program representation.
 constexpr int kMaxNodes = 32;    // configuration positions (2*order + fixed nodes)
 constexpr int kMaxDim = 32;      // Sobol dimensions per sample (2*order)
-constexpr int kMaxFixed = 3;
+constexpr int kMaxFixed = 4;
 
 // Instruction opcodes of the per-sample program.  Every thread (one qMC sample) runs
 // the same stream; matrices live in the thread's arena, column-major.
@@ -19,6 +19,7 @@ enum Opcode : uint8_t {
   OP_OMUL = 5,    // dst (=|+=) c*w * O[a] (rows x inner) * src[inner x cols]
   OP_AXPY = 6,    // dst (=|+=) c*w * src    (rows*cols elements)
   OP_LEAF = 7,    // R[a ...] += src         (rows*cols elements)
+  OP_LOADI = 8,   // dst[rows x rows] = c * identity      (root before a zero-length interval)
 };
 
 struct alignas(16) Instr {     // 32 bytes
@@ -82,6 +83,9 @@ struct DevWork {
   const uint32_t *x0;          // [D]
   const double *pts;           // optional [n_samples][D + 1]: warped points x and weights 1/q(x)
   double *sample_out;          // optional [n_samples][res_size]: per-sample integrand values
+  int32_t transform;           // QIW_TRANSFORM_* of a bare group (SORT, EXPMODEL: extras kernel)
+  int32_t pad_w;
+  double decay;                // EXPMODEL decay rate
 };
 
 // Device view of the problem data.  Tables hold i*P and i*Delta (real in the

@@ -36,6 +36,7 @@ struct Layout {
   int n = 0;
   std::vector<int> kind, op;     // per position
   std::vector<int> top_to_conf;  // topology vertex (0-based) -> position
+  std::vector<int> zero_iv;      // interval pos -> pos+1 has zero length by construction
 };
 
 struct DNode {
@@ -331,11 +332,21 @@ struct Builder {
         al.release(slot[u], dsz(u));
         continue;
       }
-      // tmp = Pm[pos][s] * V_u
-      int pmj = pmid(nu.pos, nu.s);
-      int64_t tmp = al.alloc((int64_t)d * d0);
+      // tmp = Pm[pos][s] * V_u; a zero-length interval (two fixed nodes at the same time) is
+      // the identity: no P block, tmp is V_u itself (or c * identity for an identity root)
+      const bool zero_iv = !L.zero_iv.empty() && L.zero_iv[nu.pos];
+      const bool ident_root = nu.root_top >= 0 && nu.root_op < 0;
+      int pmj = zero_iv ? -1 : pmid(nu.pos, nu.s);
+      int64_t tmp = (zero_iv && !ident_root) ? -1 : al.alloc((int64_t)d * d0);
       bool diagP = (g.kind == QIW_GROUP_BARE);
-      if (nu.root_top >= 0 && nu.root_op < 0) {
+      if (ident_root && zero_iv) {
+        Instr I = mk(OP_LOADI);
+        I.rows = (uint8_t)d;
+        I.cols = (uint8_t)d;
+        I.dst = (int32_t)tmp;
+        I.c = nu.root_c;
+        ins.push_back(I);
+      } else if (ident_root) {
         Instr I = mk(OP_LOADP);
         I.rows = (uint8_t)d;
         I.cols = (uint8_t)d;
@@ -357,16 +368,20 @@ struct Builder {
           I.c = nu.root_c;
           ins.push_back(I);
         }
-        Instr I = mk(diagP ? OP_PMULD : OP_PMUL);
-        I.rows = (uint8_t)d;
-        I.inner = (uint8_t)d;
-        I.cols = (uint8_t)d0;
-        I.dst = (int32_t)tmp;
-        I.src = (int32_t)src;
-        I.a = pmj;
-        ins.push_back(I);
-        fl += diagP ? (double)d * d0 : 2.0 * d * d * d0;
-        al.release(src, (int64_t)d * d0);
+        if (zero_iv) {
+          tmp = src;
+        } else {
+          Instr I = mk(diagP ? OP_PMULD : OP_PMUL);
+          I.rows = (uint8_t)d;
+          I.inner = (uint8_t)d;
+          I.cols = (uint8_t)d0;
+          I.dst = (int32_t)tmp;
+          I.src = (int32_t)src;
+          I.a = pmj;
+          ins.push_back(I);
+          fl += diagP ? (double)d * d0 : 2.0 * d * d * d0;
+          al.release(src, (int64_t)d * d0);
+        }
       }
       bool tmp_taken = false;
       std::vector<int> ready;
@@ -513,6 +528,14 @@ struct Builder {
           return QIW_ERR_ARG;
         }
       }
+    } else if (g.kind == QIW_GROUP_SIGMA) {
+      // PairNode(t_i) ... PairNode(t_f) (src/inchworm.jl:560-566), framed by identities at the
+      // same times: the two end intervals have zero length and are skipped by the scheduler
+      if (k < 1) {
+        *err = "self-energy groups start at order 1";
+        return QIW_ERR_ARG;
+      }
+      n = 2 * k + 2;
     } else {
       *err = "unknown group kind";
       return QIW_ERR_ARG;
@@ -532,9 +555,21 @@ struct Builder {
       out->fixed_time[out->n_fixed] = tsel;
       out->n_fixed++;
     };
+    std::vector<int> time_fixed(n, 0);
+    L.zero_iv.assign(n, 0);
     if (g.kind == QIW_GROUP_BARE) {
       fix(0, PK_IDENT, -1, T_I);
       fix(n - 1, PK_IDENT, -1, T_F);
+    } else if (g.kind == QIW_GROUP_SIGMA) {
+      fix(0, PK_IDENT, -1, T_I);
+      fix(n - 1, PK_IDENT, -1, T_F);
+      // pair vertices with fixed times: they stay pair positions of the topology
+      out->fixed_pos[out->n_fixed] = 1;
+      out->fixed_time[out->n_fixed++] = T_I;
+      out->fixed_pos[out->n_fixed] = n - 2;
+      out->fixed_time[out->n_fixed++] = T_F;
+      time_fixed[1] = time_fixed[n - 2] = 1;
+      L.zero_iv[0] = L.zero_iv[n - 2] = 1;
     } else if (g.kind == QIW_GROUP_BOLD) {
       fix(0, PK_IDENT, -1, T_I);
       fix(d_before + 1, PK_IDENT, -1, T_W);
@@ -552,11 +587,14 @@ struct Builder {
     L.top_to_conf.clear();
     out->var_pos.clear();
     for (int pos = n - 1; pos >= 0; --pos)
-      if (L.kind[pos] == PK_VAR) { L.top_to_conf.push_back(pos); out->var_pos.push_back(pos); }
+      if (L.kind[pos] == PK_VAR) {
+        L.top_to_conf.push_back(pos);
+        if (!time_fixed[pos]) out->var_pos.push_back(pos);
+      }
     out->kind = g.kind;
     out->order = k;
     out->n_nodes = n;
-    out->D = 2 * k;
+    out->D = (int)out->var_pos.size();
     out->d_before = d_before;
     out->d_after = d_after;
     out->use_bold = g.kind != QIW_GROUP_BARE;
@@ -693,7 +731,8 @@ int plan_group(const HostProblem &pb, const GroupSpec &g, const PlanOptions &opt
       case OP_LOADP: I.a = pm_off[I.a]; I.dst += (int32_t)dyn_base; break;
       case OP_PMUL:
       case OP_PMULD: I.a = pm_off[I.a]; I.dst += (int32_t)dyn_base; I.src += (int32_t)dyn_base; break;
-      case OP_LOADC: I.dst += (int32_t)dyn_base; break;
+      case OP_LOADC:
+      case OP_LOADI: I.dst += (int32_t)dyn_base; break;
       case OP_OMUL:
       case OP_AXPY: I.dst += (int32_t)dyn_base; I.src += (int32_t)dyn_base; break;
       case OP_LEAF: I.src += (int32_t)dyn_base; break;

@@ -39,8 +39,8 @@ struct Plan {
   int kind = 0, order = 0, n_nodes = 0, D = 0, d_before = 0, d_after = 0;
   int use_bold = 1;
   int n_fixed = 0;
-  int fixed_pos[kMaxFixed] = {0, 0, 0};
-  int fixed_time[kMaxFixed] = {0, 0, 0};
+  int fixed_pos[kMaxFixed] = {0, 0, 0, 0};
+  int fixed_time[kMaxFixed] = {0, 0, 0, 0};
   std::vector<int> var_pos;
   std::vector<Instr> ins;
   std::vector<PmJob> pm;

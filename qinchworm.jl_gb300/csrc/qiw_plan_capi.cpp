@@ -10,7 +10,7 @@ using namespace qiw;
 
 extern "C" int qiwp_plan(const qiw_problem_desc *pd, const qiw_group_desc *gd, int64_t arena_budget,
                          Instr *ins, int64_t ins_cap, PmJob *pm, int64_t pm_cap, WJob *wj, int64_t w_cap,
-                         int64_t *counts /* [3]: n_ins, n_pm, n_w */, int32_t *meta /* [48] */,
+                         int64_t *counts /* [3]: n_ins, n_pm, n_w */, int32_t *meta /* [64] */,
                          double *stats /* [5] */, char *err, int err_cap) {
   std::string e;
   HostProblem hp;
@@ -38,12 +38,12 @@ extern "C" int qiwp_plan(const qiw_problem_desc *pd, const qiw_group_desc *gd, i
   std::memcpy(ins, p.ins.data(), p.ins.size() * sizeof(Instr));
   std::memcpy(pm, p.pm.data(), p.pm.size() * sizeof(PmJob));
   std::memcpy(wj, p.wj.data(), p.wj.size() * sizeof(WJob));
-  std::memset(meta, 0, 48 * sizeof(int32_t));
+  std::memset(meta, 0, 64 * sizeof(int32_t));
   meta[0] = p.kind; meta[1] = p.order; meta[2] = p.n_nodes; meta[3] = p.D;
   meta[4] = p.d_before; meta[5] = p.d_after; meta[6] = p.use_bold; meta[7] = (int32_t)p.arena;
   meta[8] = p.res_size; meta[9] = p.n_fixed;
-  for (int f = 0; f < 3; ++f) { meta[10 + f] = p.fixed_pos[f]; meta[13 + f] = p.fixed_time[f]; }
-  for (size_t j = 0; j < p.var_pos.size() && j < 32; ++j) meta[16 + j] = p.var_pos[j];
+  for (int f = 0; f < kMaxFixed; ++f) { meta[10 + f] = p.fixed_pos[f]; meta[14 + f] = p.fixed_time[f]; }
+  for (size_t j = 0; j < p.var_pos.size() && j < 32; ++j) meta[18 + j] = p.var_pos[j];
   stats[0] = p.flops; stats[1] = p.tree_flops; stats[2] = (double)p.tree_leaves;
   stats[3] = (double)p.dag_nodes; stats[4] = (double)p.n_batches;
   return 0;

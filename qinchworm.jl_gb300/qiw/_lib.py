@@ -24,9 +24,13 @@ QIW_PROP_CUBIC = 1
 QIW_GROUP_BOLD = 0
 QIW_GROUP_BARE = 1
 QIW_GROUP_CORRELATOR = 2
+QIW_GROUP_SIGMA = 3
 
 QIW_PREC_FP64 = 0
 QIW_PREC_FP32 = 1
+QIW_TRANSFORM_DEFAULT = 0
+QIW_TRANSFORM_SORT = 1
+QIW_TRANSFORM_EXPMODEL = 2
 
 EXPORTS = ["qiw_ctx_create", "qiw_ctx_destroy", "qiw_last_error", "qiw_problem_set", "qiw_ppgf_set",
            "qiw_group_create", "qiw_group_stats_get", "qiw_integrate", "qiw_last_kernel_ms",
@@ -60,7 +64,7 @@ class GroupStats(C.Structure):
 
 
 class WorkDesc(C.Structure):
-    _fields_ = [("group", C.c_int32), ("reserved", C.c_int32), ("t_i", C.c_double), ("t_w", C.c_double),
+    _fields_ = [("group", C.c_int32), ("transform", C.c_int32), ("t_i", C.c_double), ("t_w", C.c_double),
                 ("t_f", C.c_double), ("first_index", C.c_uint64), ("n_samples", C.c_uint64),
                 ("n_total", C.c_uint64), ("sobol_m", C.c_void_p), ("sobol_x0", C.c_void_p)]
 

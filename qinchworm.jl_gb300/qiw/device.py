@@ -24,6 +24,7 @@ class Work:
     n_total: int = 0
     sobol_m: Optional[np.ndarray] = None
     sobol_x0: Optional[np.ndarray] = None
+    transform: int = 0             # _lib.QIW_TRANSFORM_* (bare groups; EXPMODEL takes its decay rate from t_w)
 
 
 class Device:
@@ -90,14 +91,14 @@ class Device:
         descs = (_lib.WorkDesc * len(works))()
         keep = []
         for i, w in enumerate(works):
-            order = self.group_info.get(w.group, (0, 0, 0))[1]
-            D = 2 * order
+            kind, order, _ = self.group_info.get(w.group, (0, 0, 0))
+            D = 2 * order - (2 if kind == _lib.QIW_GROUP_SIGMA else 0)   # integrated times
             m = w.sobol_m if w.sobol_m is not None else (self.sobol(D) if D else np.zeros((1, 32), np.uint32))
             x0 = w.sobol_x0 if w.sobol_x0 is not None else np.zeros(max(D, 1), np.uint32)
             m = np.ascontiguousarray(m, dtype=np.uint32)
             x0 = np.ascontiguousarray(x0, dtype=np.uint32)
             keep += [m, x0]
-            descs[i] = _lib.WorkDesc(w.group, 0, w.t_i, w.t_w, w.t_f, w.first_index, w.n_samples,
+            descs[i] = _lib.WorkDesc(w.group, w.transform, w.t_i, w.t_w, w.t_f, w.first_index, w.n_samples,
                                      w.n_total or w.n_samples, m.ctypes.data, x0.ctypes.data)
         return descs, keep
 

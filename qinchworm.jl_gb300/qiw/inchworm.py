@@ -118,13 +118,13 @@ class _Session:
         dims = self.exp.dims
         plan = []
         for td in tds:
-            if td.order > 0 and td.N_samples <= 0:
+            D = 2 * td.order - (2 if kind == _lib.QIW_GROUP_SIGMA else 0)   # integrated times
+            if D > 0 and td.N_samples <= 0:
                 plan.append(None)
                 continue
             gid = self.group(kind, td, corr)
-            D = 2 * td.order
             seqs = []
-            n_seqs = 1 if td.order == 0 else td.rand_params.N_seqs
+            n_seqs = 1 if D == 0 else td.rand_params.N_seqs
             for s in range(n_seqs):
                 if D == 0 or td.rand_params.rng is None:
                     m = self.dev.sobol(D) if D else None
@@ -139,7 +139,8 @@ class _Session:
             if p is None:
                 continue
             gid, td, seqs = p
-            start, length = rank_sub_range(td.N_samples, comm) if td.order > 0 else (0, 1)
+            exact = seqs[0][0] is None   # nothing to integrate: every rank evaluates it once
+            start, length = (0, 1) if exact else rank_sub_range(td.N_samples, comm)
             for si, (m, x0) in enumerate(seqs):
                 works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
                 index.append((gi, si))
@@ -147,7 +148,7 @@ class _Session:
         per: Dict[int, List[np.ndarray]] = {}
         for (gi, si), blocks in zip(index, res):
             v = _pack_blocks(blocks)
-            if plan[gi][1].order > 0:
+            if plan[gi][2][0][0] is not None:
                 v = comm.allreduce(v)
             per.setdefault(gi, []).append(v)
         out = []
@@ -251,6 +252,63 @@ def inchworm(expansion, orders, orders_bare, N_samples: int, n_pts_after_max: Op
         if step_callback is not None:
             step_callback(n)
     return P_orders, P_orders_std
+
+
+def diff_inchworm(expansion, orders, N_samples: int, rand_params: Optional[RandomizationParams] = None,
+                  dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm()):
+    """diff_inchworm!(expansion, grid, orders, N_samples; rand_params) (src/inchworm.jl:666-786).
+
+    Differential inchworm: at every grid point tau_n the pseudo-particle self-energy
+    Sigma(tau_n) is the sum over orders k >= 1 of the diagrams with PairNodes at tau_0 and tau_n
+    (one launch of QIW_GROUP_SIGMA groups, src/inchworm.jl:529-616); then (host, FP64)
+    conv = -i h sum_j w_j Sigma(tau_n - tau_j) P(tau_j) (trapezoid; Keldysh's integrate on the
+    imaginary branch) and P(tau_{n+1}) = P(tau_n) + h (conv - H P(tau_n)), H_s = diag(E_s + lambda)
+    (src/inchworm.jl:618-634).  With spline-interpolated P the stored Sigma lags one grid point,
+    as the reference's incremental-spline container does (it is created holding the tau_0
+    point, src/spline_gf.jl:333-336).  Writes expansion.P; returns (Sigma_orders,
+    Sigma_orders_std): order -> per-sector ImaginaryTimeGF."""
+    assert N_samples == 0 or (N_samples & (N_samples - 1)) == 0, "N_samples must be a power of 2"
+    rp = rand_params or RandomizationParams()
+    assert rp.N_seqs > 0
+    grid = expansion.grid
+    ses = _Session(dev, expansion)
+    top_data = []
+    for o in orders:
+        if o == 0:
+            continue   # no 0-th order contribution to the self-energy
+        tops = get_topologies_at_order(o, 1)
+        if tops:
+            top_data.append(TopologiesInputData(o, 1, tops, N_samples, rp))
+    sig_orders = {td.order: _zero_P(expansion) for td in top_data}
+    sig_orders_std = {td.order: _zero_P(expansion) for td in top_data}
+    H = [np.diag(P0.E).astype(np.complex128) for P0 in expansion.P0]
+    spline = bool(getattr(expansion, "interpolate_ppgf", False))
+    sigma = [np.zeros_like(P_s.data) for P_s in expansion.P]
+    h = grid.step
+    dims = expansion.dims
+    for n in range(0, grid.n_tau - 1):
+        ses.dev.set_ppgf(expansion.P)
+        res = ses.run(_lib.QIW_GROUP_SIGMA, top_data, grid.tau(0), 0.0, grid.tau(n), precision, comm)
+        value, contribs, stds = _accumulate(res, top_data, dims)
+        j_store = n + 1 if spline else n
+        if j_store < grid.n_tau:
+            for s, (sf, m) in value.items():
+                sigma[s][j_store] = m
+        new = {}
+        for s, P_s in enumerate(expansion.P):
+            P_prev = P_s.data[n]
+            conv = np.zeros_like(P_prev)
+            for j in range(0, n + 1):
+                w = 0.0 if n == 0 else (0.5 if j in (0, n) else 1.0)
+                conv = conv + w * (sigma[s][n - j] @ P_s.data[j])
+            conv = -1j * h * conv
+            new[s] = (s, P_prev + h * (conv - H[s] @ P_prev))
+        _ppgf.set_ppgf(expansion.P, n + 1, new)
+        for o in contribs:
+            for s, (sf, m) in contribs[o].items():
+                sig_orders[o][s].data[n + 1] = m
+                sig_orders_std[o][s].data[n + 1] = stds[o][s][1]
+    return sig_orders, sig_orders_std
 
 
 def correlator_2p(expansion, orders, N_samples: int, rand_params: Optional[RandomizationParams] = None,

@@ -1,7 +1,8 @@
 """Regenerates the golden fixtures in this directory from the reference's own test data.
 
 Reads (never executes) the reference repository:
-  * test/inchworm.h5           /inchworm/P/{1,2}, /inchworm/g   (written by test/inchworm.jl:180-212)
+  * test/inchworm.h5           /inchworm/P/{1,2}, /inchworm/g   (written by test/inchworm.jl:180-212),
+                                /diff_inchworm/P/{1,2}           (test/inchworm.jl:214-239)
   * test/scrambled_sobol.jl    MockRNG-scrambled Sobol vectors   (test/scrambled_sobol.jl:136-179)
   * README.md                  Z and rho of the README Anderson run (README.md:203-204)
 and writes small JSON files that the tests use on machines without the reference.
@@ -35,6 +36,8 @@ def inchworm_h5(ref: str):
                   "spline_delta": True, "interpolate_ppgf": True},
         "P": [_cplx(f.read(f"/inchworm/P/{s}")) for s in (1, 2)],
         "g": _cplx(f.read("/inchworm/g")),
+        # diff_inchworm! of the same model, orders 0:3, N = 2^8 (test/inchworm.jl:214-239)
+        "diff_P": [_cplx(f.read(f"/diff_inchworm/P/{s}")) for s in (1, 2)],
     }
     with open(os.path.join(HERE, "inchworm_h5.json"), "w") as fh:
         json.dump(out, fh, indent=1)

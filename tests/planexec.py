@@ -44,7 +44,7 @@ class HostPlan:
             pm = np.zeros(cap[1], PMJOB)
             wj = np.zeros(cap[2], WJOB)
             counts = np.zeros(3, np.int64)
-            meta = np.zeros(48, np.int32)
+            meta = np.zeros(64, np.int32)
             stats = np.zeros(5, np.float64)
             err = C.create_string_buffer(512)
             rc = plan_lib().qiwp_plan(C.byref(pd), C.byref(gd), C.c_int64(arena_budget),
@@ -63,8 +63,8 @@ class HostPlan:
         self.d_before, self.d_after, self.use_bold = int(m[4]), int(m[5]), int(m[6])
         self.arena, self.res_size, self.n_fixed = int(m[7]), int(m[8]), int(m[9])
         self.fixed_pos = [int(x) for x in m[10:10 + self.n_fixed]]
-        self.fixed_time = [int(x) for x in m[13:13 + self.n_fixed]]
-        self.var_pos = [int(x) for x in m[16:16 + self.D]]
+        self.fixed_time = [int(x) for x in m[14:14 + self.n_fixed]]
+        self.var_pos = [int(x) for x in m[18:18 + self.D]]
         self.flops, self.tree_flops, self.tree_leaves, self.dag_nodes, self.batches = stats
 
 
@@ -97,7 +97,7 @@ def execute(plan: HostPlan, exp, packed, P_tables, t_i, t_w, t_f, N, first=0, m=
         u = np.zeros((D, Ns))
         for k in range(Ns):
             u[:, k] = np.ldexp(ScrambledSobolSeq.point_uint(m, x0, first + k).astype(np.float64), -32)
-        if plan.kind == 1:
+        if plan.kind in (1, 3):   # Root: bare and self-energy groups
             acc = np.power(u[0], 1.0 / D)
             u[0] = acc
             for i in range(2, D + 1):
@@ -180,11 +180,15 @@ def execute(plan: HostPlan, exp, packed, P_tables, t_i, t_w, t_f, N, first=0, m=
             A[dst:dst + rows * cols] = (A[dst:dst + rows * cols] if accf else 0.0) + coef * A[src:src + rows * cols]
         elif op == 7:
             R[a:a + rows * cols] += A[src:src + rows * cols]
+        elif op == 8:
+            A[dst:dst + rows * rows] = 0.0
+            for r in range(rows):
+                A[dst + r * rows + r] = c
         else:
             raise ValueError(f"bad opcode {op}")
     tot = R.sum(axis=1)
     if D > 0:
-        if plan.kind == 1:
+        if plan.kind in (1, 3):
             J = math.prod([(t_f - t_i) / i for i in range(1, D + 1)])
         else:
             J = math.prod([(t_w - t_i) / i for i in range(1, plan.d_before + 1)] or [1.0]) * \
@@ -192,6 +196,8 @@ def execute(plan: HostPlan, exp, packed, P_tables, t_i, t_w, t_f, N, first=0, m=
         scale = J / N
     else:
         scale = 1.0
+    if plan.kind == 3:   # self-energy groups: +i * parity (2k - 2 integrated times)
+        scale = -scale
     out = -1j * scale * tot
     blocks, o = [], 0
     for d in dims:

@@ -219,3 +219,79 @@ def test_t2g_groups_match_oracle(device, kind, order, npa, N):
     assert _rel(got, want) < REL64
     got32 = device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32)[0]
     assert _rel(got32, want) < REL32
+
+
+@pytest.mark.parametrize("name,order", [("anderson", 1), ("anderson", 3), ("eg", 2)])
+def test_bare_domain_maps_match_oracle(device, name, order):
+    """SortTransform and ExpModelFunctionTransform on bare groups: kernel against the oracle."""
+    exp = _model(name)
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    tops = _tops(_lib.QIW_GROUP_BARE, order, 0)
+    gid = device.create_group(_lib.QIW_GROUP_BARE, order, 0, tops)
+    tl = [(x.pairs, x.parity) for x in tops]
+    ob = orc.OracleProblem(exp)
+    t_f = g.tau(5)
+    N = 256
+    decay = t_f / (2 * order)
+    for tr, kw, t_w in [(_lib.QIW_TRANSFORM_SORT, dict(transform="sort"), 0.0),
+                        (_lib.QIW_TRANSFORM_EXPMODEL, dict(transform="expmodel", decay=decay), decay)]:
+        w = [Work(gid, 0.0, t_w, t_f, 0, N, N, transform=tr)]
+        want = ob.integrate("bare", order, 0, tl, 0.0, 0.0, t_f, N, **kw)
+        assert _rel(device.integrate(w)[0], want) < REL64, tr
+        assert _rel(device.integrate(w, precision=_lib.QIW_PREC_FP32)[0], want) < REL32, tr
+
+
+def test_domain_map_arguments_are_checked(device):
+    exp = _model("anderson")
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    bare = device.create_group(_lib.QIW_GROUP_BARE, 1, 0, _tops(_lib.QIW_GROUP_BARE, 1, 0))
+    bold = device.create_group(_lib.QIW_GROUP_BOLD, 1, 1, _tops(_lib.QIW_GROUP_BOLD, 1, 1))
+    bad = [Work(bold, g.tau(0), g.tau(3), g.tau(4), 0, 64, 64, transform=_lib.QIW_TRANSFORM_SORT),
+           Work(bare, g.tau(1), 0.5, g.tau(4), 0, 64, 64, transform=_lib.QIW_TRANSFORM_EXPMODEL),
+           Work(bare, 0.0, 0.0, g.tau(4), 0, 64, 64, transform=_lib.QIW_TRANSFORM_EXPMODEL),
+           Work(bare, 0.0, 0.0, g.tau(4), 0, 64, 64, transform=7)]
+    for w in bad:
+        with pytest.raises(_lib.QiwError) as e:
+            device.integrate([w])
+        assert e.value.code == _lib.QIW_ERR_ARG
+
+
+@pytest.mark.parametrize("name,order", [("anderson", 1), ("anderson", 3), ("eg", 2), ("eg", 3)])
+def test_self_energy_groups_match_oracle(device, name, order):
+    exp = _model(name)
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    tops = get_topologies_at_order(order, 1)
+    gid = device.create_group(_lib.QIW_GROUP_SIGMA, order, 1, tops)
+    t = (g.tau(0), 0.0, g.tau(17))
+    N = 128
+    want = orc.OracleProblem(exp).integrate("sigma", order, 1, [(x.pairs, x.parity) for x in tops], *t, N)
+    assert _rel(device.integrate([Work(gid, *t, 0, N, N)])[0], want) < REL64
+    assert _rel(device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32)[0], want) < REL32
+
+
+def test_diff_inchworm_loop_matches_oracle(device):
+    from qiw.inchworm import diff_inchworm
+    exp = models.anderson(n_tau=16)
+    diff_inchworm(exp, range(0, 4), 64, dev=device)
+    pb, _ = orc.diff_inchworm(models.anderson(n_tau=16), range(0, 4), 64)
+    for s in range(len(exp.P)):
+        assert np.abs(exp.P[s].data - pb.P_data[s]).max() <= 1e-11 * np.abs(pb.P_data[s]).max()
+
+
+def test_golden_diff_inchworm_h5_through_gpu(device):
+    """The reference's fixture (test/inchworm.h5 /diff_inchworm/P, test/inchworm.jl:214-239)."""
+    import json, os
+    from qiw.inchworm import diff_inchworm
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "inchworm_h5.json")))
+    exp = models.single_level()
+    diff_inchworm(exp, range(0, 4), 2 ** 8, dev=device)
+    for s in range(2):
+        want = np.array(gold["diff_P"][s]["re"]) + 1j * np.array(gold["diff_P"][s]["im"])
+        got = exp.P[s].data[:, 0, 0]
+        assert np.linalg.norm(got - want) <= 5e-8 * np.linalg.norm(want)

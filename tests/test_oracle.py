@@ -126,6 +126,18 @@ def test_oracle_reproduces_reference_golden_inchworm():
     assert np.linalg.norm(g - want) <= 1e-6 * np.linalg.norm(want)
 
 
+def test_oracle_reproduces_reference_golden_diff_inchworm():
+    """test/inchworm.jl:214-239 (diff_inchworm!, orders 0:3, N = 2^8) via test/inchworm.h5."""
+    gold = _load("inchworm_h5.json")
+    pb, _ = orc.diff_inchworm(models.single_level(), range(0, 4), 2 ** 8)
+    for s in range(2):
+        want = np.array(gold["diff_P"][s]["re"]) + 1j * np.array(gold["diff_P"][s]["im"])
+        got = pb.P_data[s][:, 0, 0]
+        assert np.array_equal(got[:2], want[:2])            # the first Euler step is exact
+        # 1.5e-8 (norm), the residual of the bold P lookups seen in the inchworm! fixture too
+        assert np.linalg.norm(got - want) <= 5e-8 * np.linalg.norm(want)
+
+
 def test_oracle_rank_split_matches_single_rank():
     exp = models.anderson(n_tau=16)
     pb = orc.OracleProblem(exp)
@@ -135,3 +147,27 @@ def test_oracle_rank_split_matches_single_rank():
     b = pb.integrate("bold", 3, 2, tops, g.tau(0), g.tau(4), g.tau(5), 128, n_ranks=3)
     for x, y in zip(a, b):
         assert np.allclose(x, y, rtol=1e-13, atol=1e-18)
+
+
+def test_bare_domain_maps_estimate_the_same_integral():
+    """RootTransform, SortTransform and ExpModelFunctionTransform (src/qmc_integrate.jl:99-334)
+    are unbiased maps of the same simplex integral: their qMC estimates of a bare group agree
+    within the qMC error, which falls with N (test/qmc_integrate.jl checks the maps the same way,
+    against analytic integrals)."""
+    from qiw import models
+    from qiw.diagrammatics import get_topologies_at_order
+    exp = models.anderson(n_tau=40)
+    ob = orc.OracleProblem(exp)
+    t_f = exp.grid.tau(6)
+    for k, tol_sort, tol_exp in [(1, 1e-4, 2e-3), (2, 5e-4, 5e-3)]:
+        tops = [(t.pairs, t.parity) for t in get_topologies_at_order(k)]
+        errs = []
+        for N in (2 ** 12, 2 ** 16):
+            r = ob.integrate("bare", k, 0, tops, 0.0, 0.0, t_f, N)
+            s = ob.integrate("bare", k, 0, tops, 0.0, 0.0, t_f, N, transform="sort")
+            e = ob.integrate("bare", k, 0, tops, 0.0, 0.0, t_f, N, transform="expmodel", decay=t_f / (2 * k))
+            sc = max(np.abs(b).max() for b in r)
+            errs.append((max(np.abs(x - y).max() for x, y in zip(s, r)) / sc,
+                         max(np.abs(x - y).max() for x, y in zip(e, r)) / sc))
+        assert errs[1][0] < tol_sort and errs[1][1] < tol_exp, (k, errs)
+        assert errs[1][1] < errs[0][1]

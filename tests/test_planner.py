@@ -103,3 +103,19 @@ def test_offdiagonal_leaf_is_reported():
     with pytest.raises(_lib.QiwError) as ei:
         pe.HostPlan(pk, _lib.QIW_GROUP_BOLD, 1, 1, tops)
     assert ei.value.code == _lib.QIW_ERR_OFFDIAG
+
+
+@pytest.mark.parametrize("name,order", [("anderson", 1), ("anderson", 2), ("anderson", 3), ("eg", 2), ("eg", 3)])
+def test_self_energy_groups(name, order):
+    """diff_inchworm! self-energy groups: PairNodes at t_i and t_f (src/inchworm.jl:560-566)."""
+    exp = models.anderson(n_tau=30) if name == "anderson" else models.eg_discrete_bath(n_tau=30)
+    g = exp.grid
+    pk = _lib.PackedProblem(exp)
+    tops = get_topologies_at_order(order, 1)
+    hp = pe.HostPlan(pk, _lib.QIW_GROUP_SIGMA, order, 1, tops)
+    assert hp.D == 2 * order - 2 and hp.n_fixed == 4
+    t = (g.tau(0), 0.0, g.tau(13))
+    got = pe.execute(hp, exp, pk, pe.p_tables(exp), *t, 64)
+    want = orc.OracleProblem(exp).integrate("sigma", order, 1, [(x.pairs, x.parity) for x in tops], *t, 64)
+    scale = max(np.abs(w).max() for w in want)
+    assert max(np.abs(a - b).max() for a, b in zip(got, want)) <= REL * scale
