@@ -10,9 +10,9 @@ namespace qiw {
 
 constexpr int kMaxThreads = 128;     // samples per CTA (upper bound)
 #ifndef QIW_MIN_BLOCKS
-#define QIW_MIN_BLOCKS 4
+#define QIW_MIN_BLOCKS 5
 #endif
-constexpr int kMinBlocks = QIW_MIN_BLOCKS;  // 128-thread blocks per SM the register budget allows
+constexpr int kMinBlocks = QIW_MIN_BLOCKS;  // 128-thread blocks per SM: FP64 at 94 registers, no spills
 constexpr int kArenaSmall = 1024;    // per-sample arena instantiations (elements)
 constexpr int kArenaLarge = 8192;
 constexpr int kArenaHuge = 20480;   // large-sector problems (9x9 blocks); results always kResLarge
