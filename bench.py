@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--samples", type=int, default=1024)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--model", default="eg", choices=["eg", "anderson"])
+    ap.add_argument("--model", default="eg", choices=["eg", "anderson", "t2g"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy", "batch"])
     ap.add_argument("--solves", type=int, default=64, help="batch mode: independent Anderson solves")
@@ -60,10 +60,14 @@ def parse():
 
 
 def workload(model: str):
+    """(expansion, description, highest order) of a benchmark model."""
     from qiw import models
     if model == "eg":
-        return models.eg_discrete_bath(n_tau=256), "eg Kanamori U=2 J=0.2 beta=8 n_tau=256, 4-level bath"
-    return models.anderson(n_tau=200), "Anderson eps=0.1 U=1 beta=10 n_tau=200, semi-elliptic bath"
+        return models.eg_discrete_bath(n_tau=256), "eg Kanamori U=2 J=0.2 beta=8 n_tau=256, 4-level bath", 4
+    if model == "t2g":
+        return (models.t2g_bethe(n_tau=512), "t2g Kanamori U=2.3 J=0.4 beta=20 n_tau=512, semi-elliptic bath D=2 V=0.4",
+                3)
+    return models.anderson(n_tau=200), "Anderson eps=0.1 U=1 beta=10 n_tau=200, semi-elliptic bath", 4
 
 
 def bold_groups(orders, N):
@@ -170,8 +174,8 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    exp, desc = workload(args.model)
-    tds = bold_groups(range(0, 5), args.samples)
+    exp, desc, kmax = workload(args.model)
+    tds = bold_groups(range(0, kmax + 1), args.samples)
     vals = []
     for i in range(args.warmup + args.steps):
         v, cores, sample = cpu_baseline(exp, tds, args.samples, budget_s=8.0)
@@ -181,10 +185,23 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": desc + ", orders 0:4, one inch step", "N_samples": args.samples},
+            "config": {"workload": desc + f", orders 0:{kmax}, one inch step", "N_samples": args.samples},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+# DRAM bytes (read + write) of one eval_kernel launch of the default FP64 eg inch step, from one
+# ncu capture of `python bench.py --steps 2 --warmup 1 --no-cpu-baseline` (dram__bytes_read.sum
+# 21.50 GB + dram__bytes_write.sum 25.51 GB at 1024 samples, one pass): the per-thread arenas
+# spilling from L2.  It grows with the samples; other workloads report null.
+EG_FP64_TRAFFIC_PER_1024 = 47.01e9
+
+
+def _traffic(args):
+    if args.model == "eg" and args.precision == "fp64":
+        return EG_FP64_TRAFFIC_PER_1024 * args.samples / 1024
+    return None
 
 
 def run_ours(args):
@@ -202,11 +219,11 @@ def run_ours(args):
         comm = TorchComm()
     torch.cuda.set_device(local)
     prec = _lib.QIW_PREC_FP32 if args.precision == "fp32" else _lib.QIW_PREC_FP64
-    exp, desc = workload(args.model)
+    exp, desc, kmax = workload(args.model)
     grid = exp.grid
     # weak scaling: every rank evaluates N_samples per group; the step result is all-reduced
     N = args.samples
-    tds = bold_groups(range(0, 5), N * world)
+    tds = bold_groups(range(0, kmax + 1), N * world)
     dev = Device(local)
     ses = _Session(dev, exp)
     for td in tds:
@@ -217,7 +234,7 @@ def run_ours(args):
     # bare step, then warm-up and timed regular steps
     from qiw.inchworm import TopologiesInputData
     from qiw.diagrammatics import get_topologies_at_order
-    bare = [TopologiesInputData(o, 2 * o, get_topologies_at_order(o), N * world) for o in range(0, 5)]
+    bare = [TopologiesInputData(o, 2 * o, get_topologies_at_order(o), N * world) for o in range(0, kmax + 1)]
     val, _, _ = _accumulate(ses.run(_lib.QIW_GROUP_BARE, bare, grid.tau(0), 0.0, grid.tau(1), prec, comm), bare,
                             exp.dims)
     ppgf.set_ppgf(exp.P, 1, val)
@@ -273,13 +290,14 @@ def run_ours(args):
         "value": units / k_tot, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * k_tot / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64acc", "data": "synthetic",
-        "config": {"workload": desc + ", orders 0:4, one regular inch step per bench step",
+        "config": {"workload": desc + f", orders 0:{kmax}, one regular inch step per bench step",
                    "N_samples": N * world, "groups_per_step": len(tds),
                    "topologies_per_step": sum(len(td.topologies) for td in tds), "l2": "256 MB write between timed steps"},
         "e2e": {"value": units / w_tot, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * w_tot / args.steps},
         "roofline": {"bound": "fp64_pipe" if args.precision == "fp64" else "fp32_pipe", "achieved": achieved,
-                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None, "traffic": None,
+                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
+                     "traffic": _traffic(args),
                      "peak_source": "measured on this GPU: independent FMA chains on every SM (qiw_measure_fma_peak); "
                                     "MEASURED_PEAKS.json has no FP64 or FP32 CUDA-core entry",
                      "dgemm_tflops_measured": dgemm, "flops_per_step": flops_rank},
@@ -292,15 +310,21 @@ def run_ours(args):
     print(json.dumps(line))
 
 
-def _solve(model, n_tau, N, prec, dev, corr=False):
-    """Full inchworm! on the GPU; returns (P normalised by beta as arrays, G or None, seconds)."""
+def _solve(model, n_tau, N, prec, dev, corr=False, device_loop=False):
+    """Full inchworm! on the GPU; returns (P normalised by beta as arrays, G or None, seconds).
+    device_loop: the whole loop on the device (qiw.batch, one CUDA graph) instead of the host
+    loop with one launch per step; the seconds include planning either way."""
     import torch
     from qiw import models, ppgf
     from qiw.inchworm import inchworm, correlator_2p
     exp = models.eg_discrete_bath(n_tau=n_tau, corr=corr) if model == "eg" else models.anderson(n_tau=n_tau, corr=corr)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    inchworm(exp, range(0, 5), range(0, 5), N, dev=dev, precision=prec)
+    if device_loop:
+        from qiw.batch import inchworm_batch
+        inchworm_batch([exp], range(0, 5), range(0, 5), N, precision=prec, autotune=False)
+    else:
+        inchworm(exp, range(0, 5), range(0, 5), N, dev=dev, precision=prec)
     el = time.perf_counter() - t0
     ppgf.normalize_beta(exp.P, exp.grid.beta)
     G = None
@@ -329,6 +353,13 @@ def run_accuracy(args):
         P32, G32, t32 = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, corr=(N == 1024))
         row.update(err_fp64=_perr(P64, P_ref), err_fp32=_perr(P32, P_ref), s_fp64=t64, s_fp32=t32,
                    fp32_vs_fp64_P=_perr(P32, P64))
+        # the same solves with the loop on the device (warm: the first call pays the CUDA setup)
+        if N == 256:
+            _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, device_loop=True)
+        P64d, _, t64d = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP64, dev, device_loop=True)
+        P32d, _, t32d = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, device_loop=True)
+        row.update(err_fp64_dev=_perr(P64d, P_ref), err_fp32_dev=_perr(P32d, P_ref), s_fp64_dev=t64d,
+                   s_fp32_dev=t32d, dev_vs_host_P=_perr(P64d, P64))
         if G64 is not None:
             row["fp32_vs_fp64_G"] = float(np.abs(G32 - G64).max())
         sweep.append(row)
@@ -342,11 +373,16 @@ def run_accuracy(args):
 
     t64, n64 = ttt("err_fp64", "s_fp64")
     t32, n32 = ttt("err_fp32", "s_fp32")
+    t64d, n64d = ttt("err_fp64_dev", "s_fp64_dev")
+    t32d, n32d = ttt("err_fp32_dev", "s_fp32_dev")
     print(json.dumps({"mode": "accuracy", "metric": "time to 1e-4 max |P(tau) - P_ref(tau)|", "unit": "s",
                       "config": {"model": args.model, "n_tau": args.n_tau, "orders": "0:4", "N_ref": args.n_ref,
                                  "reference": "plain FP64 GPU run at N_ref (Sobol, same grid)"},
                       "time_to_1e-4_fp64": t64, "N_fp64": n64, "time_to_1e-4_fp32": t32, "N_fp32": n32,
                       "speedup_fp32": (t64 / t32) if (t64 and t32) else None,
+                      "time_to_1e-4_fp64_device_loop": t64d, "N_fp64_device_loop": n64d,
+                      "time_to_1e-4_fp32_device_loop": t32d, "N_fp32_device_loop": n32d,
+                      "speedup_fp32_device_loop_vs_plain_fp64": (t64 / t32d) if (t64 and t32d) else None,
                       "reference_solve_s": t_ref, "sweep": sweep}))
 
 
