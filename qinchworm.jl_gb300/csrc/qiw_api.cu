@@ -187,14 +187,19 @@ int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
     const int n_b = std::max(0, (int)p.batch_begin.size() - 1);
     w.n_cta = n_tiles * n_b;
     t->cta_first[i] = (int)t->cta_map.size();
-    // heaviest batches first within the work item: the block scheduler then starts the
-    // long CTAs early (the finish kernel sums the partials in this same fixed order)
+    // within the work item the batches go heaviest first; every tile has its own partial row
     std::vector<int> order(n_b);
     for (int b = 0; b < n_b; ++b) order[b] = b;
     std::stable_sort(order.begin(), order.end(),
                      [&](int x, int y) { return p.batch_flops[x] > p.batch_flops[y]; });
     for (int b : order)
-      for (int k = 0; k < n_tiles; ++k) t->cta_map.push_back(make_int4(i, b, k * threads, 0));
+      for (int k = 0; k < n_tiles; ++k) {
+        const int slot = (int)t->cta_map.size();  // partial row: the finish kernel sums a work item's rows in order
+        t->cta_map.push_back(make_int4(i, b, k * threads, slot));
+        const uint64_t s0 = (uint64_t)k * threads;
+        const double n_in = (double)std::min<uint64_t>((uint64_t)threads, w.n_samples - s0);
+        t->cta_cost.push_back(p.batch_flops[b] * n_in);
+      }
     t->res_sizes[i] = p.res_size;
     t->out_off[i] = t->out_total;
     t->out_total += p.res_size;
@@ -206,6 +211,13 @@ int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
     w.x0 = reinterpret_cast<const uint32_t *>((uintptr_t)t->sobol.size());
     if (p.D > 0) t->sobol.insert(t->sobol.end(), wd.sobol_x0, wd.sobol_x0 + p.D);
   }
+  // all tiles of the launch heaviest first: the block scheduler starts the long CTAs early
+  std::vector<size_t> ord(t->cta_map.size());
+  for (size_t k = 0; k < ord.size(); ++k) ord[k] = k;
+  std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return t->cta_cost[a] > t->cta_cost[b]; });
+  std::vector<int4> sorted(ord.size());
+  for (size_t k = 0; k < ord.size(); ++k) sorted[k] = t->cta_map[ord[k]];
+  t->cta_map.swap(sorted);
   if (!c->real_phase_problem || (need_P && !c->real_phase_P))
     return c->fail(QIW_ERR_UNSUPPORTED, "qiw_integrate: inputs are not real-phase (i*P, i*Delta and operator "
                                         "blocks must be real); only the real-phase kernels are built");

@@ -53,7 +53,8 @@ struct WarpRec;
 // Host-side launch tables of one qiw_integrate call.
 struct LaunchTables {
   std::vector<DevWork> works;         // Sobol pointers hold offsets into `sobol` until placed
-  std::vector<int4> cta_map;
+  std::vector<int4> cta_map;          // (work item, batch, first sample, partial row), heaviest first
+  std::vector<double> cta_cost;        // estimated flops of each tile (before sorting)
   std::vector<int> cta_first, res_sizes, out_off;
   std::vector<uint32_t> sobol;
   int64_t arena_max = 0;

@@ -630,11 +630,11 @@ template <typename T, int ARENA, int RESMAX, bool EXTRAS>
 __global__ void __launch_bounds__(kMaxThreads, kMinBlocks)
     eval_kernel(DevProblem pb, const DevGroup *__restrict__ groups, const DevWork *__restrict__ works,
                 const int4 *__restrict__ cta_map, double *__restrict__ partials) {
-  const int4 cm = cta_map[blockIdx.x];   // (work item, batch, first sample of the tile, -)
+  const int4 cm = cta_map[blockIdx.x];   // (work item, batch, first sample of the tile, partial row)
   const DevWork &w = works[cm.x];
   const DevGroup &g = groups[w.group];
   eval_tile<T, ARENA, RESMAX, EXTRAS>(pb, g, w, cm.y, (uint64_t)cm.z,
-                              [=]() { return partials + (size_t)blockIdx.x * g.res_size; });
+                              [=]() { return partials + (size_t)cm.w * g.res_size; });
 }
 
 }  // namespace qiw
