@@ -48,3 +48,23 @@ extern "C" int qiwp_plan(const qiw_problem_desc *pd, const qiw_group_desc *gd, i
   stats[3] = (double)p.dag_nodes; stats[4] = (double)p.n_batches;
   return 0;
 }
+
+// Per-batch flops per sample of a planned group (load-balance studies in the CPU tests).
+extern "C" int qiwp_batch_flops(const qiw_problem_desc *pd, const qiw_group_desc *gd, int64_t arena_budget,
+                                double *out, int cap) {
+  std::string e;
+  HostProblem hp;
+  GroupSpec gs;
+  int rc = host_problem_from_desc(pd, &hp, &e);
+  if (!rc) rc = group_spec_from_desc(gd, &gs, &e);
+  Plan p;
+  if (!rc) {
+    PlanOptions opt;
+    opt.arena_budget = arena_budget;
+    rc = plan_group(hp, gs, opt, &p, &e);
+  }
+  if (rc) return -rc;
+  const int n = (int)p.batch_flops.size();
+  for (int i = 0; i < n && i < cap; ++i) out[i] = p.batch_flops[i];
+  return n;
+}
