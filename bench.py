@@ -46,9 +46,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--samples", type=int, default=1024)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--model", default="eg", choices=["eg", "anderson", "t2g"])
+    ap.add_argument("--model", default="eg", choices=["eg", "anderson", "t2g", "anderson_b40"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy", "batch"])
+    ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy", "batch", "warp"])
+    ap.add_argument("--step", type=int, default=200, help="warp mode: inch step (tau_w index) the warps are fitted at")
     ap.add_argument("--solves", type=int, default=64, help="batch mode: independent Anderson solves")
     ap.add_argument("--seed", type=int, default=2024, help="batch mode: parameter seed (numpy PCG64)")
     ap.add_argument("--no-sequential", action="store_true", help="batch mode: skip the one-solve-at-a-time arm")
@@ -317,7 +318,12 @@ def _solve(model, n_tau, N, prec, dev, corr=False, device_loop=False):
     import torch
     from qiw import models, ppgf
     from qiw.inchworm import inchworm, correlator_2p
-    exp = models.eg_discrete_bath(n_tau=n_tau, corr=corr) if model == "eg" else models.anderson(n_tau=n_tau, corr=corr)
+    if model == "eg":
+        exp = models.eg_discrete_bath(n_tau=n_tau, corr=corr)
+    elif model == "anderson_b40":   # strongly correlated, low temperature: concentrated integrands
+        exp = models.anderson(eps=-2.0, U=4.0, beta=40.0, n_tau=n_tau, corr=corr)
+    else:
+        exp = models.anderson(n_tau=n_tau, corr=corr)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     if device_loop:
@@ -384,6 +390,92 @@ def run_accuracy(args):
                       "time_to_1e-4_fp32_device_loop": t32d, "N_fp32_device_loop": n32d,
                       "speedup_fp32_device_loop_vs_plain_fp64": (t64 / t32d) if (t64 and t32d) else None,
                       "reference_solve_s": t_ref, "sweep": sweep}))
+
+
+def run_warp(args):
+    """Learned warp on the eg model (beta = 8, n_tau = 256, orders 1:4): for every topology group
+    at one inch step, a warp trained on 2^16 plain-qMC samples of the group, then the variance of
+    R = 16 scrambled replicas of N = 1024 points with and without it (qiw.warp.fit_group_warp)."""
+    import torch
+    from qiw import _lib
+    from qiw.device import Device, Work
+    from qiw.diagrammatics import get_topologies_at_order
+    from qiw import warp as qwarp
+    exp, desc, kmax = workload(args.model)
+    g = exp.grid
+    dev = Device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev.set_problem(exp)
+    dev.set_ppgf(exp.P)
+    n = min(args.step, g.n_tau - 2)
+    rows = []
+    for o in range(1, kmax + 1):
+        for npa in range(1, 2 * o):
+            tops = get_topologies_at_order(o, npa)
+            if not tops or 2 * o > 8:
+                continue
+            gid = dev.create_group(_lib.QIW_GROUP_BOLD, o, npa, tops)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fit = qwarp.fit_group_warp(dev, Work(gid, g.tau(0), g.tau(n), g.tau(n + 1), 0, 0, 0), n_train=2 ** 16, R=16)
+            rows.append({"order": o, "n_pts_after": npa, "topologies": len(tops), "variance_gain": fit.gain,
+                         "kept": fit.warp_id is not None, "bias_sigma": fit.bias_sigma, "loss": fit.loss,
+                         "fit_s": time.perf_counter() - t0})
+    # the whole step: every group summed, plain vs warped (kept warps), against plain at 2^20
+    fits = {}
+    gids = []
+    for o in range(0, kmax + 1):
+        for npa in ([0] if o == 0 else range(1, 2 * o)):
+            tops = get_topologies_at_order(o, npa)
+            if tops:
+                gids.append((o, npa, dev.create_group(_lib.QIW_GROUP_BOLD, o, npa, tops)))
+    wmap = {}
+    for (o, npa, gid) in gids:
+        if o == 0 or 2 * o > 8:
+            continue
+        fit = qwarp.fit_group_warp(dev, Work(gid, g.tau(0), g.tau(n), g.tau(n + 1), 0, 0, 0), n_train=2 ** 16, R=16)
+        wmap[gid] = fit.warp_id if fit.warp_id is not None else -1
+
+    def step_total(N, prec, warped, step=n):
+        works = [Work(gid, g.tau(0), g.tau(step), g.tau(step + 1), 0, N, N) for (_, _, gid) in gids]
+        wl = [wmap.get(gid, -1) for (_, _, gid) in gids] if warped else None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = dev.integrate(works, prec, warps=wl)
+        el = time.perf_counter() - t0
+        return np.concatenate([sum(r[s] for r in res).ravel() for s in range(len(res[0]))]), el
+
+    ref, t_ref = step_total(2 ** 20, _lib.QIW_PREC_FP64, False)
+    ref_w, _ = step_total(2 ** 20, _lib.QIW_PREC_FP64, True)   # the warped estimate at the same N
+    sc = float(np.abs(ref).max())
+    sweep = []
+    N = 2 ** 10
+    while N <= 2 ** 16:
+        row = {"N": N}
+        for key, prec, warped in [("plain_fp64", _lib.QIW_PREC_FP64, False), ("warped_fp64", _lib.QIW_PREC_FP64, True),
+                                  ("warped_fp32", _lib.QIW_PREC_FP32, True)]:
+            v, el = step_total(N, prec, warped)
+            row["err_" + key] = float(np.abs(v - ref).max()) / sc
+            row["err_vs_warped_ref_" + key] = float(np.abs(v - ref_w).max()) / sc
+            row["s_" + key] = el
+        sweep.append(row)
+        N *= 2
+    # the same warps reused at later steps (no refit): does the gain persist?
+    reuse = []
+    for dn in (20, 50):
+        m = min(n + dn, g.n_tau - 2)
+        r_m, _ = step_total(2 ** 20, _lib.QIW_PREC_FP64, False, m)
+        sc_m = float(np.abs(r_m).max())
+        for Nr in (2 ** 10, 2 ** 13):
+            vp, _ = step_total(Nr, _lib.QIW_PREC_FP64, False, m)
+            vw, _ = step_total(Nr, _lib.QIW_PREC_FP32, True, m)
+            reuse.append({"step": m, "N": Nr, "err_plain_fp64": float(np.abs(vp - r_m).max()) / sc_m,
+                          "err_warped_fp32": float(np.abs(vw - r_m).max()) / sc_m})
+    print(json.dumps({"mode": "warp", "config": {"workload": desc + f", inch step tau_w index {n}",
+                                                  "train_samples": 2 ** 16, "replicas": 16, "N_per_replica": 1024,
+                                                  "step_reference": "plain FP64 at 2^20 samples per group"},
+                      "groups": rows, "reference_s": t_ref,
+                      "plain_vs_warped_at_2^20": float(np.abs(ref - ref_w).max()) / sc, "step_sweep": sweep,
+                      "reuse_at_later_steps": reuse}))
 
 
 def batch_solves(seed: int, n: int):
@@ -476,5 +568,7 @@ if __name__ == "__main__":
         run_accuracy(a)
     elif a.mode == "batch":
         run_batch(a)
+    elif a.mode == "warp":
+        run_warp(a)
     else:
         run_ours(a)

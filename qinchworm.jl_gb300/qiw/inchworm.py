@@ -317,8 +317,9 @@ def correlator_2p(expansion, orders, N_samples: int, rand_params: Optional[Rando
     """correlator_2p(expansion, grid, orders, N_samples[, RequestStdDev()]).
 
     Returns one array of <A(tau) B(0)> values on the grid per registered (A, B) pair (and the
-    standard deviations when request_std).  All tau points and groups of one correlator run
-    in a single launch: with P final, the tau points are independent."""
+    standard deviations when request_std).  All correlators, tau points and groups run in a
+    single launch: with P final, they are independent (src/inchworm.jl:1003-1045 loops over
+    them one by one)."""
     assert N_samples == 0 or (N_samples & (N_samples - 1)) == 0, "N_samples must be a power of 2"
     rp = rand_params or RandomizationParams()
     grid = expansion.grid
@@ -333,48 +334,46 @@ def correlator_2p(expansion, orders, N_samples: int, rand_params: Optional[Rando
                 top_data.append(TopologiesInputData(o, npa, tops, N_samples, rp))
     Z = _ppgf.partition_function(expansion.P)
     idx = list(range(grid.n_tau)) if taus is None else list(taus)
-    gs, stds = [], []
-    for c in range(len(expansion.corr_operators)):
+    n_c = len(expansion.corr_operators)
+    # one launch for every (correlator, tau point, group): with P final they are independent
+    all_tds, spans, per_tau, corrs = [], [], [], []
+    for c in range(n_c):
         A, B = expansion.corr_operators[c]
         assert A.is_single_monomial(), "Operator A must be a single monomial in C/C^+"
         assert B.is_single_monomial(), "Operator B must be a single monomial in C/C^+"
-        g = np.zeros(len(idx), np.complex128)
-        gstd = np.zeros(len(idx))
-        # one launch over all tau points of this correlator
-        all_tds, spans = [], []
         for q, j in enumerate(idx):
             tds = top_data[:1] if j == 0 else top_data
             if j == 0 and top_data[0].order != 0:
                 tds = []
             spans.append((q, j, len(all_tds), len(tds)))
             all_tds += tds
-        per_tau = []
-        for (q, j, a, n) in spans:
             per_tau.append((grid.tau(0), grid.tau(j), grid.tau(grid.n_tau - 1)))
-        works_res = _run_multi_tau(ses, all_tds, spans, per_tau, precision, comm, c)
-        for (q, j, a, n), r in zip(spans, works_res):
-            val, sd = 0j, 0.0
-            for (mean, std), td in r:
-                val += sum(np.trace(b) for b in mean)
-                if td.order > 0:
-                    sd += float(np.real(sum(np.trace(b) for b in std)))
-            g[q] = val / Z
-            gstd[q] = sd / Z.real
-        gs.append(g)
-        stds.append(gstd)
+            corrs.append(c)
+    works_res = _run_multi_tau(ses, all_tds, spans, per_tau, precision, comm, corrs)
+    gs = [np.zeros(len(idx), np.complex128) for _ in range(n_c)]
+    stds = [np.zeros(len(idx)) for _ in range(n_c)]
+    for (q, j, a, n), c, r in zip(spans, corrs, works_res):
+        val, sd = 0j, 0.0
+        for (mean, std), td in r:
+            val += sum(np.trace(b) for b in mean)
+            if td.order > 0:
+                sd += float(np.real(sum(np.trace(b) for b in std)))
+        gs[c][q] = val / Z
+        stds[c][q] = sd / Z.real
     return (gs, stds) if request_std else gs
 
 
-def _run_multi_tau(ses: _Session, all_tds, spans, times, precision, comm, corr):
-    """Runs the correlator groups of every tau point in one qiw_integrate call."""
+def _run_multi_tau(ses: _Session, all_tds, spans, times, precision, comm, corrs):
+    """Runs the correlator groups of every span (correlator corrs[i], one tau point) in one
+    qiw_integrate call."""
     dims = ses.exp.dims
     works, index = [], []
-    for (q, j, a, n), (t_i, t_w, t_f) in zip(spans, times):
+    for si, ((q, j, a, n), (t_i, t_w, t_f)) in enumerate(zip(spans, times)):
         for k in range(n):
             td = all_tds[a + k]
             if td.order > 0 and td.N_samples <= 0:
                 continue
-            gid = ses.group(_lib.QIW_GROUP_CORRELATOR, td, corr)
+            gid = ses.group(_lib.QIW_GROUP_CORRELATOR, td, corrs[si])
             D = 2 * td.order
             n_seqs = 1 if td.order == 0 else td.rand_params.N_seqs
             for s in range(n_seqs):
@@ -384,19 +383,19 @@ def _run_multi_tau(ses: _Session, all_tds, spans, times, precision, comm, corr):
                     m, x0 = scramble(ses.dev.sobol(D), td.rand_params.rng)
                 start, length = rank_sub_range(td.N_samples, comm) if td.order > 0 else (0, 1)
                 works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
-                index.append((q, a + k))
+                index.append((si, a + k))
     res = ses.dev.integrate(works, precision) if works else []
     grouped: Dict[Tuple[int, int], List[np.ndarray]] = {}
-    for (q, ti), blocks in zip(index, res):
+    for (si, ti), blocks in zip(index, res):
         v = _pack_blocks(blocks)
         if all_tds[ti].order > 0:
             v = comm.allreduce(v)
-        grouped.setdefault((q, ti), []).append(v)
+        grouped.setdefault((si, ti), []).append(v)
     out = []
-    for (q, j, a, n) in spans:
+    for si, (q, j, a, n) in enumerate(spans):
         r = []
         for k in range(n):
-            vs = np.array(grouped.get((q, a + k), []))
+            vs = np.array(grouped.get((si, a + k), []))
             if len(vs) == 0:
                 continue
             mean = vs.mean(axis=0)
