@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--n-tau", type=int, default=32, help="accuracy mode: tau grid size")
     ap.add_argument("--n-ref", type=int, default=2 ** 15, help="accuracy mode: samples of the FP64 reference")
     ap.add_argument("--n-max", type=int, default=2 ** 13, help="accuracy mode: largest swept N")
+    ap.add_argument("--warp-n-max", type=int, default=0, help="accuracy mode: largest N of the warped FP32 arm (0: off)")
+    ap.add_argument("--warp-refit", type=int, default=16, help="accuracy mode: refit the warps every this many steps")
     return ap.parse_args()
 
 
@@ -311,7 +313,7 @@ def run_ours(args):
     print(json.dumps(line))
 
 
-def _solve(model, n_tau, N, prec, dev, corr=False, device_loop=False):
+def _solve(model, n_tau, N, prec, dev, corr=False, device_loop=False, warp_policy=None):
     """Full inchworm! on the GPU; returns (P normalised by beta as arrays, G or None, seconds).
     device_loop: the whole loop on the device (qiw.batch, one CUDA graph) instead of the host
     loop with one launch per step; the seconds include planning either way."""
@@ -330,7 +332,7 @@ def _solve(model, n_tau, N, prec, dev, corr=False, device_loop=False):
         from qiw.batch import inchworm_batch
         inchworm_batch([exp], range(0, 5), range(0, 5), N, precision=prec, autotune=False)
     else:
-        inchworm(exp, range(0, 5), range(0, 5), N, dev=dev, precision=prec)
+        inchworm(exp, range(0, 5), range(0, 5), N, dev=dev, precision=prec, warp_policy=warp_policy)
     el = time.perf_counter() - t0
     ppgf.normalize_beta(exp.P, exp.grid.beta)
     G = None
@@ -371,6 +373,16 @@ def run_accuracy(args):
         sweep.append(row)
         N *= 2
 
+    warped = []
+    if args.warp_n_max:
+        from qiw.warp import WarpPolicy
+        pol = WarpPolicy(refit_every=args.warp_refit)
+        N = 256
+        while N <= args.warp_n_max:
+            Pw, _, tw = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, warp_policy=pol)
+            warped.append({"N": N, "err_warped_fp32": _perr(Pw, P_ref), "s_warped_fp32": tw})
+            N *= 2
+
     def ttt(key_err, key_t):
         for r in sweep:
             if r[key_err] <= 1e-4:
@@ -389,7 +401,8 @@ def run_accuracy(args):
                       "time_to_1e-4_fp64_device_loop": t64d, "N_fp64_device_loop": n64d,
                       "time_to_1e-4_fp32_device_loop": t32d, "N_fp32_device_loop": n32d,
                       "speedup_fp32_device_loop_vs_plain_fp64": (t64 / t32d) if (t64 and t32d) else None,
-                      "reference_solve_s": t_ref, "sweep": sweep}))
+                      "reference_solve_s": t_ref, "sweep": sweep, "warped_sweep": warped,
+                      "warp_refit_every": args.warp_refit}))
 
 
 def run_warp(args):

@@ -113,8 +113,9 @@ class _Session:
         return g
 
     def run(self, kind: int, tds: Sequence[TopologiesInputData], t_i, t_w, t_f, precision, comm: Comm,
-            corr: Optional[int] = None):
-        """All groups of a step; returns per group (mean blocks, std blocks or None)."""
+            corr: Optional[int] = None, warps: Optional[Dict[int, int]] = None):
+        """All groups of a step; returns per group (mean blocks, std blocks or None).  `warps`
+        maps a group id to a learned warp its samples are drawn through."""
         dims = self.exp.dims
         plan = []
         for td in tds:
@@ -144,7 +145,15 @@ class _Session:
             for si, (m, x0) in enumerate(seqs):
                 works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
                 index.append((gi, si))
-        res = self.dev.integrate(works, precision) if works else []
+        wl = [warps.get(w.group, -1) for w in works] if warps else None
+        if wl is not None and all(x < 0 for x in wl):
+            wl = None
+        if not works:
+            res = []
+        elif wl is None:
+            res = self.dev.integrate(works, precision)
+        else:
+            res = self.dev.integrate(works, precision, warps=wl)
         per: Dict[int, List[np.ndarray]] = {}
         for (gi, si), blocks in zip(index, res):
             v = _pack_blocks(blocks)
@@ -206,12 +215,14 @@ def _zero_P(expansion):
 def inchworm(expansion, orders, orders_bare, N_samples: int, n_pts_after_max: Optional[int] = None,
              rand_params: Optional[RandomizationParams] = None, dev: Optional[Device] = None,
              precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm(), n_steps: Optional[int] = None,
-             step_callback=None):
+             step_callback=None, warp_policy=None):
     """inchworm!(expansion, grid, orders, orders_bare, N_samples; n_pts_after_max, rand_params).
 
     Writes the bold propagator into expansion.P and returns (P_orders, P_orders_std):
     dict order -> list of per-sector ImaginaryTimeGF.  `n_steps` stops after that many
-    regular steps (the remaining grid points keep their atomic values)."""
+    regular steps (the remaining grid points keep their atomic values).  `warp_policy`
+    (qiw.warp.WarpPolicy) draws the samples of each bold group through a learned warp, refitted
+    every few steps and kept only where it lowers the variance; the estimates stay unbiased."""
     assert N_samples == 0 or (N_samples & (N_samples - 1)) == 0, "N_samples must be a power of 2"
     rp = rand_params or RandomizationParams()
     assert rp.N_seqs > 0
@@ -239,9 +250,26 @@ def inchworm(expansion, orders, orders_bare, N_samples: int, n_pts_after_max: Op
                 top_bold.append(TopologiesInputData(o, npa, tops, N_samples, rp))
 
     last = grid.n_tau - 1 if n_steps is None else min(grid.n_tau - 1, 1 + n_steps)
+    warps: Dict[int, int] = {}
     for n in range(1, last):
         ses.dev.set_ppgf(expansion.P)
-        res = ses.run(_lib.QIW_GROUP_BOLD, top_bold, grid.tau(0), grid.tau(n), grid.tau(n + 1), precision, comm)
+        if warp_policy is not None and n >= warp_policy.first_step and \
+                (n - warp_policy.first_step) % warp_policy.refit_every == 0:
+            from .warp import fit_group_warp
+            for td in top_bold:
+                if td.order == 0 or 2 * td.order > 8:
+                    continue
+                gid = ses.group(_lib.QIW_GROUP_BOLD, td)
+                fit = fit_group_warp(ses.dev, Work(gid, grid.tau(0), grid.tau(n), grid.tau(n + 1), 0, 0, 0),
+                                     n_train=warp_policy.n_train, steps=warp_policy.train_steps,
+                                     uniform_mix=warp_policy.uniform_mix, N_test=warp_policy.N_test,
+                                     R=warp_policy.R, min_gain=warp_policy.min_gain)
+                if fit.warp_id is None:
+                    warps.pop(gid, None)
+                else:
+                    warps[gid] = fit.warp_id
+        res = ses.run(_lib.QIW_GROUP_BOLD, top_bold, grid.tau(0), grid.tau(n), grid.tau(n + 1), precision, comm,
+                      warps=warps)
         value, contribs, stds = _accumulate(res, top_bold, expansion.dims)
         _ppgf.set_ppgf(expansion.P, n + 1, value)
         _ppgf.normalize_tau(expansion.P, n + 1)  # suppress exponential growth (src/inchworm.jl:488)

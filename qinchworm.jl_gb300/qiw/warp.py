@@ -22,6 +22,20 @@ from .sobol import NumpyBitRNG, direction_numbers, scramble, sobol_points
 
 
 @dataclass
+class WarpPolicy:
+    """When inchworm() fits warps: at step first_step and every refit_every steps after it, for
+    every bold group of order >= 1 (2*order <= 8), kept only where they lower the variance."""
+    refit_every: int = 16
+    first_step: int = 4
+    n_train: int = 2 ** 15
+    train_steps: int = 600
+    uniform_mix: float = 0.3
+    N_test: int = 1024
+    R: int = 8
+    min_gain: float = 1.0
+
+
+@dataclass
 class WarpFit:
     warp_id: Optional[int]      # None: plain qMC is the better estimator
     gain: float                 # measured variance ratio plain / warped

@@ -87,3 +87,23 @@ def test_warp_dropped_where_plain_qmc_is_better(device):
     fit = qwarp.fit_group_warp(device, Work(gid, g.tau(0), g.tau(16), g.tau(17), 0, 0, 0))
     assert fit.bias_sigma <= 4
     assert fit.gain < 1 and fit.warp_id is None
+
+
+def test_inchworm_with_warp_policy_is_unbiased(device):
+    """Whole inchworm! with warps refitted every few steps (kept where they lower the variance):
+    the result stays an estimate of the same P -- its error against a plain 2^15 reference is
+    of the plain run's size or smaller."""
+    from qiw.inchworm import inchworm
+    from qiw.warp import WarpPolicy
+
+    def solve(N, policy=None):
+        exp = models.eg_discrete_bath(n_tau=24)
+        inchworm(exp, range(0, 4), range(0, 4), N, dev=device, warp_policy=policy)
+        return [P_s.data.copy() for P_s in exp.P]
+
+    ref = solve(2 ** 15)
+    err = lambda P: max(np.abs(a - b).max() for a, b in zip(P, ref))
+    e_plain = err(solve(1024))
+    e_warp = err(solve(1024, WarpPolicy(refit_every=6, first_step=4, n_train=2 ** 14, R=8)))
+    print(f"eg n_tau=24, N=1024: error plain {e_plain:.2e}, warped {e_warp:.2e}")
+    assert np.isfinite(e_warp) and e_warp < 1.5 * e_plain
