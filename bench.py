@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--model", default="eg", choices=["eg", "anderson", "t2g", "anderson_b40"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy", "batch", "warp"])
+    ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy", "batch", "warp", "correlators"])
     ap.add_argument("--step", type=int, default=200, help="warp mode: inch step (tau_w index) the warps are fitted at")
     ap.add_argument("--solves", type=int, default=64, help="batch mode: independent Anderson solves")
     ap.add_argument("--seed", type=int, default=2024, help="batch mode: parameter seed (numpy PCG64)")
@@ -491,6 +491,39 @@ def run_warp(args):
                       "reuse_at_later_steps": reuse}))
 
 
+def run_correlators(args):
+    """inchworm! then correlator_2p (G(tau) and <S+(tau) S->) on the t2g model, FP64 and FP32
+    chains, with the FP32 error of P and of every correlator against the FP64 path (which the
+    parity tests tie to the oracle group by group).  n_tau and N from --n-tau / --samples."""
+    import torch
+    from qiw import _lib, models, ppgf
+    from qiw.device import Device
+    from qiw.inchworm import correlator_2p, inchworm
+    dev = Device(int(os.environ.get("LOCAL_RANK", "0")))
+    out = {}
+    for name, prec in (("fp64", _lib.QIW_PREC_FP64), ("fp32", _lib.QIW_PREC_FP32)):
+        exp = models.t2g_bethe(n_tau=args.n_tau, corr=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        inchworm(exp, range(0, 4), range(0, 4), args.samples, dev=dev, precision=prec)
+        t1 = time.perf_counter()
+        ppgf.normalize_beta(exp.P, exp.grid.beta)
+        gs = correlator_2p(exp, range(0, 4), args.samples, dev=dev, precision=prec)
+        t2 = time.perf_counter()
+        out[name] = ([P_s.data.copy() for P_s in exp.P], [np.asarray(g) for g in gs], t1 - t0, t2 - t1)
+    P64, G64, ti64, tc64 = out["fp64"]
+    P32, G32, ti32, tc32 = out["fp32"]
+    print(json.dumps({"mode": "correlators", "config": {"workload": f"t2g Kanamori U=2.3 J=0.4 beta=20 n_tau={args.n_tau}, "
+                                                        "orders 0:3, correlators G(tau) and <S+(tau) S-> of orbital 1",
+                                                        "N_samples": args.samples},
+                      "inchworm_s": {"fp64": ti64, "fp32": ti32}, "correlator_2p_s": {"fp64": tc64, "fp32": tc32},
+                      "fp32_max_abs_dP": _perr(P32, P64), "P_max_abs": max(float(np.abs(p).max()) for p in P64),
+                      "fp32_max_abs_dG": [float(np.abs(a - b).max()) for a, b in zip(G32, G64)],
+                      "G_max_abs": [float(np.abs(g).max()) for g in G64],
+                      "G_fp64_tau0_beta": [[[complex(g[0]).real, complex(g[0]).imag], [complex(g[-1]).real, complex(g[-1]).imag]]
+                                           for g in G64]}))
+
+
 def batch_solves(seed: int, n: int):
     """Seed-drawn Anderson solves: beta U[2, 40], n_tau U{64..512}, U U[0.5, 4], eps U[-1, 1],
     V U[0.2, 1], D = 2, max order U{2..6}, N = 2^U{8..14} (numpy PCG64)."""
@@ -583,5 +616,7 @@ if __name__ == "__main__":
         run_batch(a)
     elif a.mode == "warp":
         run_warp(a)
+    elif a.mode == "correlators":
+        run_correlators(a)
     else:
         run_ours(a)

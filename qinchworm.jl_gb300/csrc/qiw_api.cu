@@ -138,7 +138,7 @@ int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
   t->cta_first.assign(n_work, 0);
   t->res_sizes.assign(n_work, 0);
   t->out_off.assign(n_work, 0);
-  const int threads = c->threads;
+  const int threads = c->threads;  // samples per tile
   for (int i = 0; i < n_work; ++i) {
     const qiw_work_desc &wd = work[i];
     if (wd.group < 0 || wd.group >= (int)c->groups.size()) return c->fail(QIW_ERR_ARG, "qiw_integrate: bad group id");

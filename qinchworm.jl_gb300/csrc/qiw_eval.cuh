@@ -395,20 +395,12 @@ struct TileSrc {
 // the CTA's partial sums at partial_row()[0 .. res_size).  Every thread of the CTA must call it.
 // EXTRAS compiles in the warped points and the per-sample output (qiw_integrate_warped /
 // qiw_integrate_samples); the plain kernels are built without them (fewer live registers).
-template <typename T, int ARENA, int RESMAX, bool EXTRAS, typename Src, typename RowFn>
-__device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &g, const Src &w, int batch,
-                                          uint64_t s0, RowFn partial_row) {
-  const uint64_t sidx = s0 + threadIdx.x;
-  bool active = sidx < w.n_samples;   // cleared for samples a domain map discards
-  const int res_size = g.res_size;
-
-  T A[ARENA];
-  double R[RESMAX];
-#pragma unroll 1
-  for (int e = 0; e < res_size; ++e) R[e] = 0.0;
-
-  double wt = 1.0;
-  if (active) {
+// Per-sample setup of one tile slot: Sobol point (or warped point), domain map, the i*P blocks
+// of the intervals the program uses and the i*Delta weights, into the sample's arena A.
+// `active` is cleared for samples a domain map discards; `wt` collects per-sample weights.
+template <typename T, bool EXTRAS, typename Src>
+__device__ __forceinline__ void sample_setup(const DevProblem &pb, const DevGroup &g, const Src &w,
+                                             uint64_t sidx, T *__restrict__ A, double &wt, bool &active) {
     double tm[kMaxNodes];
     const double tsel[3] = {w.t_i, w.t_w, w.t_f};
 #pragma unroll 1
@@ -552,6 +544,19 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
 
   }
 
+template <typename T, int ARENA, int RESMAX, bool EXTRAS, typename Src, typename RowFn>
+__device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &g, const Src &w, int batch,
+                                          uint64_t s0, RowFn partial_row) {
+  const int res_size = g.res_size;
+  const uint64_t sidx = s0 + threadIdx.x;
+  bool active = sidx < w.n_samples;   // cleared for samples a domain map discards
+  double wt = 1.0;
+  T A[ARENA];
+  double R[RESMAX];
+#pragma unroll 1
+  for (int e = 0; e < res_size; ++e) R[e] = 0.0;
+  if (active) sample_setup<T, EXTRAS>(pb, g, w, sidx, A, wt, active);
+
   // The group's program: the instructions of this CTA's batch.  Scalar programs (all blocks
   // 1x1) stream them through shared memory in chunks of blockDim.x: each thread copies one
   // 32-byte instruction of the next chunk with cp.async while the current chunk executes (the
@@ -616,7 +621,6 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
     if (lane == 0) red[warp][e] = v;
   }
   __syncthreads();
-#pragma unroll 1
   double *prow = partial_row();  // formed only now: nothing holds it across the tile
 #pragma unroll 1
   for (int e = threadIdx.x; e < res_size; e += blockDim.x) {
