@@ -376,7 +376,7 @@ def run_accuracy(args):
     warped = []
     if args.warp_n_max:
         from qiw.warp import WarpPolicy
-        pol = WarpPolicy(refit_every=args.warp_refit)
+        pol = WarpPolicy(refit_every=args.warp_refit, n_train=2 ** 14)
         N = 256
         while N <= args.warp_n_max:
             Pw, _, tw = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, warp_policy=pol)
@@ -389,6 +389,17 @@ def run_accuracy(args):
                 return r[key_t], r["N"]
         return None, None
 
+    def first_below(rows, key_err, key_t, tol):
+        for r in rows:
+            if r[key_err] <= tol:
+                return r[key_t], r["N"]
+        return None, None
+
+    thresholds = {}
+    for tol in (3e-2, 1e-2, 3e-3, 1e-3, 1e-4):
+        thresholds[f"{tol:g}"] = {"plain_fp64": first_below(sweep, "err_fp64", "s_fp64", tol),
+                                  "fp32_device_loop": first_below(sweep, "err_fp32_dev", "s_fp32_dev", tol),
+                                  "warped_fp32": first_below(warped, "err_warped_fp32", "s_warped_fp32", tol)}
     t64, n64 = ttt("err_fp64", "s_fp64")
     t32, n32 = ttt("err_fp32", "s_fp32")
     t64d, n64d = ttt("err_fp64_dev", "s_fp64_dev")
@@ -402,6 +413,7 @@ def run_accuracy(args):
                       "time_to_1e-4_fp32_device_loop": t32d, "N_fp32_device_loop": n32d,
                       "speedup_fp32_device_loop_vs_plain_fp64": (t64 / t32d) if (t64 and t32d) else None,
                       "reference_solve_s": t_ref, "sweep": sweep, "warped_sweep": warped,
+                      "time_to_error": thresholds,
                       "warp_refit_every": args.warp_refit}))
 
 
