@@ -305,8 +305,8 @@ int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
     delete g;
     return c->fail(QIW_ERR_MEMORY, "qiw_group_create: per-sample arena above the largest kernel instantiation");
   }
-  // flag bit 0 = (c != 1); the FP32 copy holds c rounded to float in the low 4 bytes of c
-  for (Instr &I : g->plan.ins) I.flags = (I.c != 1.0) ? 1 : 0;
+  // flag bits: 0 = (c != 1), 1 = (c == -1); the FP32 copy holds c rounded to float in the low 4 bytes of c
+  for (Instr &I : g->plan.ins) I.flags = (uint8_t)((I.c != 1.0 ? 1 : 0) | (I.c == -1.0 ? 2 : 0));
   std::vector<Instr> ins32(g->plan.ins);
   for (Instr &I : ins32) {
     const float f = (float)I.c;

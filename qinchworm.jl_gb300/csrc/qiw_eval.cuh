@@ -212,7 +212,17 @@ template <>
 __device__ __forceinline__ float coef_c<float>(const Instr &I) {
   return __int_as_float((int)(unsigned)(__double_as_longlong(I.c) & 0xffffffffull));
 }
-__device__ __forceinline__ bool has_c(const Instr &I) { return (I.flags & 1u) != 0; }
+__device__ __forceinline__ bool has_c(const Instr &I) { return (I.flags & 1u) != 0; }  // bit 1: c == -1
+
+// Coefficient of an edge: c (flag bit 0: c != 1) times the per-sample weight A[w] when w >= 0.
+// c == -1 exactly (flag bit 1) is a sign flip, which the consuming FMA takes for free.
+template <typename T>
+__device__ __forceinline__ T edge_coef(const Instr &I, const T *A) {
+  if (I.w < 0) return coef_c<T>(I);
+  const T w = A[I.w];
+  if (!has_c(I)) return w;
+  return (I.flags & 2u) ? -w : coef_c<T>(I) * w;
+}
 
 // Programs whose blocks are all 1x1 (single-orbital models): about 1.5 flops per
 // instruction, so decoding and fetching the stream dominate; this executor has one short path
@@ -238,7 +248,7 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
       if (I.w < 0 && !has_c(I)) {
         A[I.dst] = I.acc ? fmaT<T>(o, x, A[I.dst]) : o * x;
       } else {
-        const T coef = (I.w >= 0) ? (has_c(I) ? coef_c<T>(I) * A[I.w] : A[I.w]) : coef_c<T>(I);
+        const T coef = edge_coef<T>(I, A);
         const T p = o * x;
         A[I.dst] = I.acc ? fmaT<T>(coef, p, A[I.dst]) : coef * p;
       }
@@ -249,7 +259,7 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
       if (I.w < 0 && !has_c(I)) {
         A[I.dst] = I.acc ? x + A[I.dst] : x;
       } else {
-        const T coef = (I.w >= 0) ? (has_c(I) ? coef_c<T>(I) * A[I.w] : A[I.w]) : coef_c<T>(I);
+        const T coef = edge_coef<T>(I, A);
         A[I.dst] = I.acc ? fmaT<T>(coef, x, A[I.dst]) : coef * x;
       }
       break;
@@ -330,7 +340,7 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
     case OP_OMUL: {
       const int inner = I.inner;
       const bool has_coef = (I.w >= 0) || has_c(I);
-      const T coef = (I.w >= 0) ? (has_c(I) ? coef_c<T>(I) * A[I.w] : A[I.w]) : coef_c<T>(I);
+      const T coef = edge_coef<T>(I, A);
       const int cr = dcode(rows), ck = dcode(inner), cc = dcode(cols);
       if (cr >= 0 && ck >= 0 && cc >= 0) {
         const int code = cr * 9 + ck * 3 + cc;
@@ -351,7 +361,7 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
     }
     case OP_AXPY: {
       const bool has_coef = (I.w >= 0) || has_c(I);
-      const T coef = (I.w >= 0) ? (has_c(I) ? coef_c<T>(I) * A[I.w] : A[I.w]) : coef_c<T>(I);
+      const T coef = edge_coef<T>(I, A);
       const int n = rows * cols;
       const bool accf = I.acc != 0;
       switch (n) {
