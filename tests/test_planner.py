@@ -119,3 +119,26 @@ def test_self_energy_groups(name, order):
     want = orc.OracleProblem(exp).integrate("sigma", order, 1, [(x.pairs, x.parity) for x in tops], *t, 64)
     scale = max(np.abs(w).max() for w in want)
     assert max(np.abs(a - b).max() for a, b in zip(got, want)) <= REL * scale
+
+
+def test_batch_flops_add_up_to_the_plan():
+    """Per-batch flop counts (the load-balancing cost of a tile) sum, with the per-sample P and
+    Delta lookups, to the plan's flops per sample."""
+    import ctypes as C
+    exp = models.eg_discrete_bath(n_tau=30)
+    pk = _lib.PackedProblem(exp)
+    pd = pk.desc()
+    lib = pe.plan_lib()
+    lib.qiwp_batch_flops.restype = C.c_int
+    lib.qiwp_batch_flops.argtypes = [C.POINTER(_lib.ProblemDesc), C.POINTER(_lib.GroupDesc), C.c_int64,
+                                     C.c_void_p, C.c_int]
+    for order, npa in [(2, 2), (3, 3), (4, 4)]:
+        tops = get_topologies_at_order(order, npa)
+        gd, keep = _lib.pack_group(_lib.QIW_GROUP_BOLD, order, npa, tops)
+        out = np.zeros(4096)
+        n = lib.qiwp_batch_flops(C.byref(pd), C.byref(gd), 8192, out.ctypes.data, out.size)
+        hp = pe.HostPlan(pk, _lib.QIW_GROUP_BOLD, order, npa, tops)
+        assert n == int(hp.batches) and np.all(out[:n] > 0)
+        dims = np.array(exp.dims)
+        lookups = sum(3.0 * dims[int(j["s"])] ** 2 for j in hp.pm) + 3.0 * len(hp.wj)
+        assert abs(out[:n].sum() + lookups - hp.flops) <= 1e-9 * hp.flops
