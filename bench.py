@@ -307,7 +307,7 @@ def run_ours(args):
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,
     }
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1:   # the CPU leg runs at N = 1 only
         v, cores, sample = cpu_baseline(exp, tds, N)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     print(json.dumps(line))
