@@ -295,3 +295,26 @@ def test_golden_diff_inchworm_h5_through_gpu(device):
         want = np.array(gold["diff_P"][s]["re"]) + 1j * np.array(gold["diff_P"][s]["im"])
         got = exp.P[s].data[:, 0, 0]
         assert np.linalg.norm(got - want) <= 5e-8 * np.linalg.norm(want)
+
+
+def test_readme_anderson_output_through_gpu(device):
+    """The reference README's workflow (README.md:51-125: Anderson model, inchworm! orders 0:4,
+    bare 0:4, N = 2^10, n_tau = 200) against its printed rho (README.md:204).
+
+    The printed Z = 22.515 (README.md:203) is not reproduced by the reference's current
+    inchworm!: after every step it rescales P so that max_s,i -Im P_s,ii(tau_f) = 1
+    (src/inchworm.jl:489 with src/ppgf.jl:646-654), so at tau_f = beta the un-normalized
+    Z = sum_s Tr[i P_s(beta)] equals 1 / max_s rho_s exactly.  The test asserts that identity."""
+    import json, os
+    from qiw import ppgf
+    from qiw.inchworm import inchworm
+    ra = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "readme_anderson.json")))
+    exp = models.anderson()
+    inchworm(exp, range(0, 5), range(0, 5), 2 ** 10, dev=device)
+    Z = ppgf.partition_function(exp.P)
+    ppgf.normalize_beta(exp.P, exp.grid.beta)
+    rho = [float(np.real(m[0, 0])) for m in ppgf.density_matrix(exp.P)]
+    print(f"README run: Z = {Z.real:.10f}, rho = {rho} (README {ra['rho']})")
+    assert abs(Z.imag) < 1e-12
+    assert abs(Z.real * max(rho) - 1.0) < 1e-10
+    assert np.allclose(rho, ra["rho"], atol=1e-4)
