@@ -2,8 +2,9 @@
 
 These are synthetic inputs in the reference's own parametrisation: the README Anderson
 model (`README.md:51-99`), the Kanamori Hamiltonian of
-`bench/two_band_eg_model_discrete_bath/two_band_eg_model_discrete_bath.jl:36-56`, and the
-single-level model of the reference's `test/inchworm.jl:55-212` fixture.
+`bench/two_band_eg_model_discrete_bath/two_band_eg_model_discrete_bath.jl:36-56`, the
+single-level model of the reference's `test/inchworm.jl:55-212` fixture, and the two dimers
+that the reference checks against exact diagonalisation (`test/dimers.jl`).
 """
 from __future__ import annotations
 
@@ -53,6 +54,28 @@ def single_level(beta: float = 10.0, mu: float = 0.1, eps: float = 0.1, V: float
     grid = ImaginaryTimeGrid(beta, n_tau)
     Delta = V ** 2 * gf_from_dos(DeltaDOS.make([eps]), grid)
     return Expansion(ed, grid, _diag_pairs([("0",)], [Delta], spline=spline), interpolate_ppgf=spline)
+
+
+def dimer(beta: float = 1.0, eps_1: float = 0.5, eps_2: float = 2.0, V: float = 0.5,
+          n_tau: int = 32, spline: bool = False) -> Expansion:
+    """Level 1 (H = eps_1 n_1) hybridised with one bath level eps_2 (test/dimers.jl:35-90);
+    ``spline`` selects the SplineInterpolatedGF / interpolate_ppgf variant of :68-72."""
+    ed = EDCore(eps_1 * op.n(1), op.SetOfIndices([[1]]))
+    grid = ImaginaryTimeGrid(beta, n_tau)
+    Delta = V ** 2 * gf_from_dos(DeltaDOS.make([eps_2]), grid)
+    return Expansion(ed, grid, _diag_pairs([(1,)], [Delta], spline=spline), interpolate_ppgf=spline)
+
+
+def hubbard_dimer(beta: float = 1.0, U: float = 4.0, eps_2: float = 0.0, V: float = 0.5,
+                  n_tau: int = 32) -> Expansion:
+    """Hubbard atom at half filling (eps_1 = -U/2) with one bath level per spin
+    (test/dimers.jl:118-175)."""
+    eps_1 = -0.5 * U
+    H = U * op.n(1) * op.n(2) + eps_1 * (op.n(1) + op.n(2))
+    ed = EDCore(H, op.SetOfIndices([[1], [2]]))
+    grid = ImaginaryTimeGrid(beta, n_tau)
+    Delta = V ** 2 * gf_from_dos(DeltaDOS.make([eps_2]), grid)
+    return Expansion(ed, grid, _diag_pairs([(1,), (2,)], [Delta, Delta]))
 
 
 def kanamori_hamiltonian(n_orb: int, mu: float, U: float, J: float):
