@@ -119,6 +119,16 @@ typedef struct {
 
 int qiw_group_stats_get(qiw_ctx *ctx, int32_t group_id, qiw_group_stats *out);
 
+/* Plan cache of the process.  qiw_group_create (and qiw_batch_add) keep every plan they make,
+ * keyed by the operator structure of the problem (sector dimensions, operator blocks and
+ * values, pair operators) and the group (kind, order, n_pts_after, correlator operators,
+ * topologies, parities).  Plans hold no times or tables, so a solve repeated with a new Delta,
+ * beta or grid on the same operators (an outer self-consistency loop around inchworm!) plans
+ * no group again, in any context or batch.  Thread-safe.  The cache is emptied when it would
+ * exceed 2 GiB of host memory, or by qiw_plan_cache_clear. */
+int qiw_plan_cache_info(int64_t *entries, int64_t *hits, int64_t *bytes);
+int qiw_plan_cache_clear(void);
+
 /* Domain maps of a bare group (src/qmc_integrate.jl): the default is RootTransform (:198-258);
  * SortTransform (:282-334) maps x to t_i + sort(x, rev=true) (t_f - t_i); ExpModelFunctionTransform
  * (:99-165) maps x to u_1 = t_f + tau log(1 - x_1), u_n = u_{n-1} + tau log(1 - x_n) with the

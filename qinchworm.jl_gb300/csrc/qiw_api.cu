@@ -6,7 +6,10 @@
 #include <complex>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "qiw_ctx.hpp"
@@ -281,32 +284,79 @@ int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const De
 
 namespace qiw {
 
-// Plans a group on c's problem, uploads its program and fills its device descriptor.
+// Process-wide store of host plans by plan_key + planner budget.  Plans are immutable once
+// stored and hold no times or tables, so every context and batch of the process shares them:
+// repeated solves on one operator structure (new Delta, beta or grid) plan each group once.
+constexpr int64_t kPlanCacheBytes = (int64_t)1 << 31;
+
+struct PlanStore {
+  std::mutex m;
+  std::unordered_map<std::string, std::shared_ptr<const Plan>> map;
+  int64_t bytes = 0, hits = 0;
+};
+
+PlanStore &plan_store() {
+  static PlanStore store;
+  return store;
+}
+
+std::shared_ptr<const Plan> plan_store_find(const std::string &key) {
+  PlanStore &ps = plan_store();
+  std::lock_guard<std::mutex> lock(ps.m);
+  auto it = ps.map.find(key);
+  if (it == ps.map.end()) return nullptr;
+  ps.hits++;
+  return it->second;
+}
+
+void plan_store_insert(std::string &&key, const Plan &p) {
+  const int64_t bytes = (int64_t)(p.ins.size() * sizeof(Instr) + p.pm.size() * sizeof(PmJob) +
+                                  p.wj.size() * sizeof(WJob) + key.size());
+  auto sp = std::make_shared<const Plan>(p);
+  PlanStore &ps = plan_store();
+  std::lock_guard<std::mutex> lock(ps.m);
+  if (ps.bytes + bytes > kPlanCacheBytes) {
+    ps.map.clear();
+    ps.bytes = 0;
+  }
+  if (ps.map.emplace(std::move(key), std::move(sp)).second) ps.bytes += bytes;
+}
+
+// Plans a group on c's problem (or takes the plan from c's cache), uploads its program and
+// fills its device descriptor.
 int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
   PlanOptions opt;
   opt.arena_budget = kArenaLarge;
   if (const char *b = std::getenv("QIW_ARENA_BUDGET")) opt.arena_budget = std::max<int64_t>(256, std::atoll(b));
   opt.arena_budget = std::min<int64_t>(opt.arena_budget, kArenaLarge);
+  std::string key = plan_key(c->hp, gs);
+  key.append(reinterpret_cast<const char *>(&opt.arena_budget), sizeof(opt.arena_budget));
   GroupRec *g = new GroupRec();
-  std::string e;
-  int rc = plan_group(c->hp, gs, opt, &g->plan, &e);
-  if (rc == QIW_ERR_MEMORY && opt.arena_budget == kArenaLarge) {
-    // large sector blocks: one (topology, sector) tree needs more than the large arena
-    opt.arena_budget = kArenaHuge;
-    e.clear();
-    g->plan = Plan();
-    rc = plan_group(c->hp, gs, opt, &g->plan, &e);
+  if (std::shared_ptr<const Plan> hit = plan_store_find(key)) {
+    g->plan = *hit;
+  } else {
+    std::string e;
+    int rc = plan_group(c->hp, gs, opt, &g->plan, &e);
+    if (rc == QIW_ERR_MEMORY && opt.arena_budget == kArenaLarge) {
+      // large sector blocks: one (topology, sector) tree needs more than the large arena
+      opt.arena_budget = kArenaHuge;
+      e.clear();
+      g->plan = Plan();
+      rc = plan_group(c->hp, gs, opt, &g->plan, &e);
+    }
+    if (rc) {
+      delete g;
+      return c->fail(rc, "qiw_group_create: " + e);
+    }
+    if (arena_class(g->plan.arena) < 0) {
+      delete g;
+      return c->fail(QIW_ERR_MEMORY, "qiw_group_create: per-sample arena above the largest kernel instantiation");
+    }
+    // flag bits: 0 = (c != 1), 1 = (c == -1)
+    for (Instr &I : g->plan.ins) I.flags = (uint8_t)((I.c != 1.0 ? 1 : 0) | (I.c == -1.0 ? 2 : 0));
+    plan_store_insert(std::move(key), g->plan);
   }
-  if (rc) {
-    delete g;
-    return c->fail(rc, "qiw_group_create: " + e);
-  }
-  if (arena_class(g->plan.arena) < 0) {
-    delete g;
-    return c->fail(QIW_ERR_MEMORY, "qiw_group_create: per-sample arena above the largest kernel instantiation");
-  }
-  // flag bits: 0 = (c != 1), 1 = (c == -1); the FP32 copy holds c rounded to float in the low 4 bytes of c
-  for (Instr &I : g->plan.ins) I.flags = (uint8_t)((I.c != 1.0 ? 1 : 0) | (I.c == -1.0 ? 2 : 0));
+  // the FP32 copy holds c rounded to float in the low 4 bytes of c
   std::vector<Instr> ins32(g->plan.ins);
   for (Instr &I : ins32) {
     const float f = (float)I.c;
@@ -315,6 +365,7 @@ int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
     std::memcpy(&I.c, &bits, sizeof(bits));
   }
   const Plan &p = g->plan;
+  int rc;
   if ((rc = c->cuda(g->pm.upload(p.pm.data(), p.pm.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(g->wj.upload(p.wj.data(), p.wj.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(g->ins.upload(p.ins.data(), p.ins.size(), c->stream), "upload plan")) ||
@@ -530,6 +581,23 @@ int qiw_group_create(qiw_ctx *c, const qiw_group_desc *d, int32_t *group_id) {
   c->groups.push_back(g);
   c->groups_dirty = true;
   *group_id = (int32_t)c->groups.size() - 1;
+  return QIW_OK;
+}
+
+int qiw_plan_cache_info(int64_t *entries, int64_t *hits, int64_t *bytes) {
+  PlanStore &ps = plan_store();
+  std::lock_guard<std::mutex> lock(ps.m);
+  if (entries) *entries = (int64_t)ps.map.size();
+  if (hits) *hits = ps.hits;
+  if (bytes) *bytes = ps.bytes;
+  return QIW_OK;
+}
+
+int qiw_plan_cache_clear(void) {
+  PlanStore &ps = plan_store();
+  std::lock_guard<std::mutex> lock(ps.m);
+  ps.map.clear();
+  ps.bytes = 0;
   return QIW_OK;
 }
 

@@ -48,35 +48,6 @@ struct TileSet {
   int slots = 0, res_total = 0;
 };
 
-void append_bytes(std::string *k, const void *p, size_t n) { k->append(reinterpret_cast<const char *>(p), n); }
-
-template <typename T>
-void append_vec(std::string *k, const std::vector<T> &v) {
-  const uint64_t n = v.size();
-  append_bytes(k, &n, sizeof(n));
-  if (n) append_bytes(k, v.data(), n * sizeof(T));
-}
-
-// Everything a group program depends on: the operator structure of the problem and the group.
-std::string plan_key(const HostProblem &hp, const GroupSpec &gs) {
-  std::string k;
-  append_bytes(&k, &hp.S, sizeof(hp.S));
-  append_vec(&k, hp.dims);
-  append_bytes(&k, &hp.n_ops, sizeof(hp.n_ops));
-  append_vec(&k, hp.op_target);
-  append_vec(&k, hp.op_valoff);
-  append_vec(&k, hp.op_vals);
-  append_bytes(&k, &hp.identity_op, sizeof(hp.identity_op));
-  append_bytes(&k, &hp.n_pairs, sizeof(hp.n_pairs));
-  append_vec(&k, hp.pair_op_i);
-  append_vec(&k, hp.pair_op_f);
-  const int g[5] = {gs.kind, gs.order, gs.n_pts_after, gs.corr_A, gs.corr_B};
-  append_bytes(&k, g, sizeof(g));
-  for (const auto &t : gs.tops) append_vec(&k, t);
-  append_vec(&k, gs.parity);
-  return k;
-}
-
 }  // namespace
 
 struct qiw_batch {

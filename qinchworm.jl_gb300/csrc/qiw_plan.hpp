@@ -60,6 +60,12 @@ struct Plan {
 int plan_group(const HostProblem &pb, const GroupSpec &g, const PlanOptions &opt, Plan *out,
                std::string *err);
 
+// Everything a group program depends on, as bytes: the operator structure of the problem
+// (sector dimensions, block targets and values, pair operators) and the group (kind, order,
+// n_pts_after, correlator operators, topologies, parities).  Equal keys give equal plans for
+// equal PlanOptions; the times, P and Delta tables are not part of a plan.
+std::string plan_key(const HostProblem &hp, const GroupSpec &gs);
+
 }  // namespace qiw
 
 namespace qiw {

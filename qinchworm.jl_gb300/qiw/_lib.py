@@ -37,7 +37,8 @@ EXPORTS = ["qiw_ctx_create", "qiw_ctx_destroy", "qiw_last_error", "qiw_problem_s
            "qiw_measure_fma_peak", "qiw_integrate_noalloc", "qiw_warp_create", "qiw_warp_set_mix", "qiw_warp_n_params",
            "qiw_warp_get_params", "qiw_warp_set_params", "qiw_warp_grad", "qiw_warp_train", "qiw_warp_map",
            "qiw_integrate_warped", "qiw_integrate_samples", "qiw_batch_create", "qiw_batch_destroy",
-           "qiw_batch_last_error", "qiw_batch_add", "qiw_batch_run", "qiw_batch_get_P", "qiw_batch_stats_get"]
+           "qiw_batch_last_error", "qiw_batch_add", "qiw_batch_run", "qiw_batch_get_P", "qiw_batch_stats_get",
+           "qiw_plan_cache_info", "qiw_plan_cache_clear"]
 
 QIW_BATCH_GRAPH = 1
 QIW_BATCH_AUTOTUNE = 2
@@ -103,6 +104,8 @@ def load(path: Optional[str] = None) -> C.CDLL:
     lib.qiw_ppgf_set.argtypes = [C.c_void_p, C.c_void_p]
     lib.qiw_group_create.argtypes = [C.c_void_p, C.POINTER(GroupDesc), C.POINTER(C.c_int32)]
     lib.qiw_group_stats_get.argtypes = [C.c_void_p, C.c_int32, C.POINTER(GroupStats)]
+    lib.qiw_plan_cache_info.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.qiw_plan_cache_clear.argtypes = []
     lib.qiw_integrate.argtypes = [C.c_void_p, C.c_int32, C.POINTER(WorkDesc), C.c_int32, C.c_void_p]
     lib.qiw_last_kernel_ms.argtypes = [C.c_void_p]
     lib.qiw_last_kernel_ms.restype = C.c_double

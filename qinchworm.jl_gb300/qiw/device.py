@@ -81,6 +81,15 @@ class Device:
         self._check(self.lib.qiw_group_stats_get(self.h, gid, C.byref(st)))
         return st
 
+    def plan_cache_info(self) -> dict:
+        """Entries, hits and host bytes of the process's plan cache (qiw_plan_cache_info)."""
+        e, h, b = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self.lib.qiw_plan_cache_info(C.byref(e), C.byref(h), C.byref(b)))
+        return {"entries": e.value, "hits": h.value, "bytes": b.value}
+
+    def plan_cache_clear(self) -> None:
+        self._check(self.lib.qiw_plan_cache_clear())
+
     def sobol(self, D: int) -> np.ndarray:
         if D not in self._sobol_cache:
             self._sobol_cache[D] = np.ascontiguousarray(direction_numbers(D), dtype=np.uint32)

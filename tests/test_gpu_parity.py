@@ -318,3 +318,43 @@ def test_readme_anderson_output_through_gpu(device):
     assert abs(Z.imag) < 1e-12
     assert abs(Z.real * max(rho) - 1.0) < 1e-10
     assert np.allclose(rho, ra["rho"], atol=1e-4)
+
+
+def test_plan_cache_reuses_plans_across_problems(device):
+    """qiw_plan_cache_*: a second solve on the same operators (new Delta, beta, grid) plans no
+    group again and gives the same P as a solve with an empty cache; operators with other
+    block values (eg Kanamori with another J rotates the eigenbasis) are planned anew; a
+    batch reuses the plans of the host-driven loop."""
+    from qiw.inchworm import inchworm
+    device.plan_cache_clear()
+    a = models.anderson(n_tau=16, V=0.5)
+    inchworm(a, range(0, 4), range(0, 4), 64, dev=device)
+    i1 = device.plan_cache_info()
+    b = models.anderson(n_tau=20, V=0.6, beta=5.0)
+    inchworm(b, range(0, 4), range(0, 4), 64, dev=device)
+    i2 = device.plan_cache_info()
+    assert i1["entries"] > 0 and i2["entries"] == i1["entries"]
+    assert i2["hits"] - i1["hits"] >= i1["entries"]
+    device.plan_cache_clear()
+    assert device.plan_cache_info()["entries"] == 0
+    c = models.anderson(n_tau=20, V=0.6, beta=5.0)
+    inchworm(c, range(0, 4), range(0, 4), 64, dev=device)
+    for s in range(len(b.P)):
+        assert np.array_equal(b.P[s].data, c.P[s].data)
+    device.plan_cache_clear()
+    inchworm(models.eg_discrete_bath(n_tau=8, J=0.2), range(0, 3), range(0, 3), 64, dev=device)
+    e1 = device.plan_cache_info()
+    inchworm(models.eg_discrete_bath(n_tau=8, J=0.3), range(0, 3), range(0, 3), 64, dev=device)
+    e2 = device.plan_cache_info()
+    assert e2["entries"] > e1["entries"]
+    from qiw.batch import inchworm_batch
+    device.plan_cache_clear()
+    h = models.anderson(n_tau=20, V=0.6, beta=5.0)
+    inchworm(h, range(0, 4), range(0, 4), 64, dev=device)
+    i3 = device.plan_cache_info()
+    d = models.anderson(n_tau=20, V=0.6, beta=5.0)
+    inchworm_batch([d], range(0, 4), range(0, 4), 64, autotune=False)
+    i4 = device.plan_cache_info()
+    assert i4["entries"] == i3["entries"] and i4["hits"] > i3["hits"]
+    for s in range(len(h.P)):
+        assert np.abs(h.P[s].data - d.P[s].data).max() <= 1e-12 * np.abs(h.P[s].data).max()
