@@ -53,27 +53,47 @@ struct DEdge {
   int u, v, op, w;               // op: -1 identity; w: weight triple id or -1
 };
 
-typedef std::vector<int32_t> KeyVec;
+// Most arcs a state can hold (open + future <= order), and the packing limit of a position,
+// a sector or a pair index in one byte of an arc word.
+constexpr int kMaxArcs = 16;
 
-std::string key_str(const KeyVec &k) {
-  return std::string(reinterpret_cast<const char *>(k.data()), k.size() * sizeof(int32_t));
-}
-
-// A state: (s0, s, open arcs (tail, pair), future arcs (head, tail)).
+// A state: (s0, s, open arcs (tail, pair), future arcs (head, tail)).  Each arc is one word
+// (first << 8 | second), so the ascending word order is the lexicographic order of the pairs.
 struct State {
-  int s0, s;
-  std::vector<std::pair<int, int>> open;
-  std::vector<std::pair<int, int>> fut;
-  KeyVec key() const {
-    KeyVec k;
-    k.reserve(4 + 2 * (open.size() + fut.size()));
-    k.push_back(s0);
-    k.push_back(s);
-    k.push_back((int)open.size());
-    for (auto &o : open) { k.push_back(o.first); k.push_back(o.second); }
-    k.push_back((int)fut.size());
-    for (auto &f : fut) { k.push_back(f.first); k.push_back(f.second); }
-    return k;
+  int s0 = 0, s = 0;
+  int n_open = 0, n_fut = 0;
+  uint16_t open[kMaxArcs];
+  uint16_t fut[kMaxArcs];
+
+  static void insert(uint16_t *a, int *n, uint16_t v) {
+    int i = *n;
+    while (i > 0 && a[i - 1] > v) { a[i] = a[i - 1]; --i; }
+    a[i] = v;
+    ++*n;
+  }
+  static void erase(uint16_t *a, int *n, int k) {
+    for (int i = k; i + 1 < *n; ++i) a[i] = a[i + 1];
+    --*n;
+  }
+  bool operator==(const State &o) const {
+    return s0 == o.s0 && s == o.s && n_open == o.n_open && n_fut == o.n_fut &&
+           std::memcmp(open, o.open, n_open * sizeof(uint16_t)) == 0 &&
+           std::memcmp(fut, o.fut, n_fut * sizeof(uint16_t)) == 0;
+  }
+};
+
+struct StateHash {
+  size_t operator()(const State &st) const {
+    uint64_t h = 0x9e3779b97f4a7c15ull;
+    auto mix = [&h](uint64_t v) {
+      h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+      h *= 0xff51afd7ed558ccdull;
+    };
+    mix((uint64_t)(uint32_t)st.s0 << 32 | (uint32_t)st.s);
+    mix((uint64_t)st.n_open << 8 | (uint64_t)st.n_fut);
+    for (int i = 0; i < st.n_open; ++i) mix(st.open[i]);
+    for (int i = 0; i < st.n_fut; ++i) mix((uint64_t)st.fut[i] << 16);
+    return (size_t)(h ^ (h >> 33));
   }
 };
 
@@ -124,8 +144,8 @@ struct Builder {
   const GroupSpec &g;
   const PlanOptions &opt;
   Layout L;
-  std::map<std::pair<int, int>, int> pm_slot;      // (iv, s) -> Pm job index
-  std::map<std::tuple<int, int, int>, int> w_slot; // (head, tail, pair) -> W job index
+  // job ids in order of first use: (iv, s) -> Pm job, (head, tail, pair) -> W job (-1: none yet)
+  std::vector<int> pm_slot, w_slot;
   std::vector<std::tuple<int, int, int>> w_list;
   std::vector<std::pair<int, int>> pm_list;
   std::string *err;
@@ -134,21 +154,21 @@ struct Builder {
       : pb(p), g(gs), opt(o), err(e) {}
 
   int wid(int h, int t, int p) {
-    auto k = std::make_tuple(h, t, p);
-    auto it = w_slot.find(k);
-    if (it != w_slot.end()) return it->second;
-    int id = (int)w_list.size();
+    const size_t k = ((size_t)h * L.n + t) * pb.n_pairs + p;
+    if (w_slot.empty()) w_slot.assign((size_t)L.n * L.n * std::max(pb.n_pairs, 1), -1);
+    if (w_slot[k] >= 0) return w_slot[k];
+    const int id = (int)w_list.size();
     w_slot[k] = id;
-    w_list.push_back(k);
+    w_list.emplace_back(h, t, p);
     return id;
   }
   int pmid(int iv, int s) {
-    auto k = std::make_pair(iv, s);
-    auto it = pm_slot.find(k);
-    if (it != pm_slot.end()) return it->second;
-    int id = (int)pm_list.size();
+    const size_t k = (size_t)iv * pb.S + s;
+    if (pm_slot.empty()) pm_slot.assign((size_t)L.n * pb.S, -1);
+    if (pm_slot[k] >= 0) return pm_slot[k];
+    const int id = (int)pm_list.size();
     pm_slot[k] = id;
-    pm_list.push_back(k);
+    pm_list.emplace_back(iv, s);
     return id;
   }
 
@@ -158,15 +178,14 @@ struct Builder {
     nodes.clear();
     edges.clear();
     states.clear();
-    std::vector<std::unordered_map<std::string, int>> maps(L.n);
-    auto get = [&](int pos, State &&st) -> int {
-      std::string k = key_str(st.key());
-      auto it = maps[pos].find(k);
+    std::vector<std::unordered_map<State, int, StateHash>> maps(L.n);
+    auto get = [&](int pos, const State &st) -> int {
+      auto it = maps[pos].find(st);
       if (it != maps[pos].end()) return it->second;
       int id = (int)nodes.size();
-      maps[pos].emplace(std::move(k), id);
+      maps[pos].emplace(st, id);
       nodes.push_back(DNode{pos, st.s0, st.s});
-      states.push_back(std::move(st));
+      states.push_back(st);
       return id;
     };
     std::vector<int> layer;
@@ -186,9 +205,8 @@ struct Builder {
           *err = "topology arc with tail not above head (pos_tail > pos_head violated)";
           return QIW_ERR_ARG;
         }
-        st.fut.emplace_back(ph, ptl);
+        State::insert(st.fut, &st.n_fut, (uint16_t)(ph << 8 | ptl));
       }
-      std::sort(st.fut.begin(), st.fut.end());
       int root_op = -1;
       if (L.kind[0] == PK_OPER) {
         root_op = L.op[0];
@@ -200,7 +218,7 @@ struct Builder {
         *err = "position 0 must hold a fixed node";
         return QIW_ERR_ARG;
       }
-      int id = get(0, std::move(st));
+      int id = get(0, st);
       nodes[id].root_top = t;
       nodes[id].root_op = root_op;
       nodes[id].root_c = (double)g.parity[t];
@@ -210,60 +228,53 @@ struct Builder {
       std::vector<int> next;
       for (int u : layer) {
         const State cur = states[u];
-        auto add_edge = [&](State &&st, int op, int w) {
-          int v = get(pos, std::move(st));
+        auto add_edge = [&](const State &st, int op, int w) {
+          int v = get(pos, st);
           edges.push_back(DEdge{u, v, op, w});
           nodes[u].out.push_back((int)edges.size() - 1);
           nodes[v].n_in++;
           if (nodes[v].n_in == 1) next.push_back(v);
         };
         if (L.kind[pos] == PK_IDENT) {
-          State st = cur;
-          add_edge(std::move(st), -1, -1);
+          add_edge(cur, -1, -1);
         } else if (L.kind[pos] == PK_OPER) {
           int t = pb.target(L.op[pos], cur.s);
           if (t >= 0) {
             State st = cur;
             st.s = t;
-            add_edge(std::move(st), L.op[pos], -1);
+            add_edge(st, L.op[pos], -1);
           }
         } else {
           int fi = -1;
-          for (size_t k = 0; k < cur.fut.size(); ++k)
-            if (cur.fut[k].first == pos) fi = (int)k;
+          for (int k = 0; k < cur.n_fut; ++k)
+            if ((cur.fut[k] >> 8) == pos) fi = k;
           if (fi >= 0) {
-            int tail = cur.fut[fi].second;
+            const int tail = cur.fut[fi] & 0xff;
+            State base = cur;
+            State::erase(base.fut, &base.n_fut, fi);
             for (int p = 0; p < pb.n_pairs; ++p) {
               int t = pb.target(pb.pair_op_i[p], cur.s);
               if (t < 0) continue;
-              State st;
-              st.s0 = cur.s0;
+              State st = base;
               st.s = t;
-              st.open = cur.open;
-              st.open.emplace_back(tail, p);
-              std::sort(st.open.begin(), st.open.end());
-              st.fut = cur.fut;
-              st.fut.erase(st.fut.begin() + fi);
-              add_edge(std::move(st), pb.pair_op_i[p], wid(pos, tail, p));
+              State::insert(st.open, &st.n_open, (uint16_t)(tail << 8 | p));
+              add_edge(st, pb.pair_op_i[p], wid(pos, tail, p));
             }
           } else {
             int oi = -1;
-            for (size_t k = 0; k < cur.open.size(); ++k)
-              if (cur.open[k].first == pos) oi = (int)k;
+            for (int k = 0; k < cur.n_open; ++k)
+              if ((cur.open[k] >> 8) == pos) oi = k;
             if (oi < 0) {
               *err = "configuration position is neither an arc head nor an arc tail";
               return QIW_ERR_ARG;
             }
-            int p = cur.open[oi].second;
+            int p = cur.open[oi] & 0xff;
             int t = pb.target(pb.pair_op_f[p], cur.s);
             if (t >= 0) {
-              State st;
-              st.s0 = cur.s0;
+              State st = cur;
               st.s = t;
-              st.open = cur.open;
-              st.open.erase(st.open.begin() + oi);
-              st.fut = cur.fut;
-              add_edge(std::move(st), pb.pair_op_f[p], -1);
+              State::erase(st.open, &st.n_open, oi);
+              add_edge(st, pb.pair_op_f[p], -1);
             }
           }
         }
@@ -316,6 +327,7 @@ struct Builder {
     const int last = L.n - 1;
     double fl = 0.0;
     auto mk = [](uint8_t op) { Instr I; std::memset(&I, 0, sizeof(I)); I.op = op; I.w = -1; I.c = 1.0; return I; };
+    std::vector<int> ready;
     while (!stack.empty()) {
       int u = stack.back();
       stack.pop_back();
@@ -384,7 +396,7 @@ struct Builder {
         }
       }
       bool tmp_taken = false;
-      std::vector<int> ready;
+      ready.clear();
       for (int e : nu.out) {
         const DEdge &E = edges[e];
         if (!nodes[E.v].alive) continue;
@@ -652,6 +664,10 @@ int plan_group(const HostProblem &pb, const GroupSpec &g, const PlanOptions &opt
   Builder B(pb, g, opt, err);
   int rc = B.setup_layout(out);
   if (rc) return rc;
+  if (g.order > kMaxArcs || B.L.n > 256 || pb.n_pairs > 256) {
+    *err = "group beyond the planner's packing limits (order <= 16, <= 256 positions and pairs)";
+    return QIW_ERR_UNSUPPORTED;
+  }
   std::vector<int> res_off(pb.S);
   int ro = 0;
   for (int s = 0; s < pb.S; ++s) { res_off[s] = ro; ro += pb.dims[s] * pb.dims[s]; }
