@@ -5,10 +5,12 @@
 // and piecewise linear on K equal bins, q_d(x) = v_b + (v_{b+1} - v_b) t (t the position in
 // bin b), with knot heights v = (1 - a) e^l / S + a normalised to unit integral (S) and mixed
 // with the uniform density (a), logits l = l_d(x_<d) from a masked MLP (MADE: D inputs, 3
-// hidden layers of 64 ReLU units, D*(K+1) outputs; output d sees inputs < d only).  The CDF
+// hidden layers of 64 tanh units, D*(K+1) outputs; output d sees inputs < d only).  The CDF
 // is quadratic per bin and is inverted in closed form.  q(x) = prod_d q_d, so the estimator
 // (1/N) sum_i f(u(x_i)) J / q(x_i) is unbiased for every set of weights; because q is
-// continuous the warped integrand stays continuous, which keeps quasi-Monte Carlo effective.  Training
+// continuous the warped integrand stays continuous, which keeps quasi-Monte Carlo effective; the
+// smooth activation keeps the conditioner l_d(x_<d) smooth as well (ReLU units would add kinks
+// along oblique hyperplanes of x_<d, which qMC points resolve poorly).  Training
 // minimises the |f|-weighted negative log-likelihood -sum_i w_i log q(x_i) of samples x_i
 // produced by plain qMC (w_i = |f(x_i)|), i.e. fits q to |f|.  Weights are stored in BF16
 // (FP32 master copy for Adam); all arithmetic accumulates in FP32.
@@ -47,7 +49,7 @@ struct Layout {
   }
 };
 
-__device__ __forceinline__ float relu(float x) { return x > 0.f ? x : 0.f; }
+__device__ __forceinline__ float act(float x) { return tanhf(x); }
 
 // Weights (BF16 on the device) -> FP32 in shared memory.
 __device__ void load_weights(const __nv_bfloat16 *wq, float *sw, int n) {
@@ -81,21 +83,21 @@ __global__ void made_grad_kernel(const __nv_bfloat16 *__restrict__ wq, int D, fl
     const int s = i / WH, j = i % WH;
     float a = W[L.ob1 + j];
     for (int k = 0; k < D; ++k) a = fmaf(W[L.oW1 + j * D + k], x[s * WDMAX + k], a);
-    h1[i] = relu(a);
+    h1[i] = act(a);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < WTILE * WH; i += blockDim.x) {
     const int s = i / WH, j = i % WH;
     float a = W[L.ob2 + j];
     for (int k = 0; k < WH; ++k) a = fmaf(W[L.oW2 + j * WH + k], h1[s * WH + k], a);
-    h2[i] = relu(a);
+    h2[i] = act(a);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < WTILE * WH; i += blockDim.x) {
     const int s = i / WH, j = i % WH;
     float a = W[L.ob3 + j];
     for (int k = 0; k < WH; ++k) a = fmaf(W[L.oW3 + j * WH + k], h2[s * WH + k], a);
-    h3[i] = relu(a);
+    h3[i] = act(a);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < WTILE * L.DK; i += blockDim.x) {
@@ -154,7 +156,7 @@ __global__ void made_grad_kernel(const __nv_bfloat16 *__restrict__ wq, int D, fl
     const int s = i / WH, j = i % WH;
     float a = 0.f;
     for (int o = 0; o < L.DK; ++o) a = fmaf(W[L.oW4 + o * WH + j], dl[s * L.DK + o], a);
-    dB[i] = h3[i] > 0.f ? a : 0.f;
+    dB[i] = a * (1.f - h3[i] * h3[i]);
   }
   __syncthreads();
   // W3, b3, dh2 (into h3)
@@ -173,7 +175,7 @@ __global__ void made_grad_kernel(const __nv_bfloat16 *__restrict__ wq, int D, fl
     const int s = i / WH, j = i % WH;
     float a = 0.f;
     for (int o = 0; o < WH; ++o) a = fmaf(W[L.oW3 + o * WH + j], dB[s * WH + o], a);
-    h3[i] = h2[i] > 0.f ? a : 0.f;
+    h3[i] = a * (1.f - h2[i] * h2[i]);
   }
   __syncthreads();
   // W2, b2, dh1 (into dB)
@@ -193,7 +195,7 @@ __global__ void made_grad_kernel(const __nv_bfloat16 *__restrict__ wq, int D, fl
     const int s = i / WH, j = i % WH;
     float a = 0.f;
     for (int o = 0; o < WH; ++o) a = fmaf(W[L.oW2 + o * WH + j], h3[s * WH + o], a);
-    dB[i] = h1[i] > 0.f ? a : 0.f;
+    dB[i] = a * (1.f - h1[i] * h1[i]);
   }
   __syncthreads();
   // W1, b1
@@ -252,17 +254,17 @@ __global__ void warp_map_kernel(const __nv_bfloat16 *__restrict__ wq, int D, flo
     for (int j = 0; j < WH; ++j) {
       float a = sw[L.ob1 + j];
       for (int k = 0; k < D; ++k) a = fmaf(sw[L.oW1 + j * D + k], xin[k], a);
-      h1[j] = relu(a);
+      h1[j] = act(a);
     }
     for (int j = 0; j < WH; ++j) {
       float a = sw[L.ob2 + j];
       for (int k = 0; k < WH; ++k) a = fmaf(sw[L.oW2 + j * WH + k], h1[k], a);
-      h2[j] = relu(a);
+      h2[j] = act(a);
     }
     for (int j = 0; j < WH; ++j) {
       float a = sw[L.ob3 + j];
       for (int k = 0; k < WH; ++k) a = fmaf(sw[L.oW3 + j * WH + k], h2[k], a);
-      h3[j] = relu(a);
+      h3[j] = act(a);
     }
     float v[WKP], mx = -1e30f;
     for (int c = 0; c < WKP; ++c) {
@@ -365,7 +367,7 @@ int qiw_warp_create(qiw_ctx *c, int32_t D, uint64_t seed, int32_t *warp_id) {
   std::mt19937_64 rng(seed);
   std::normal_distribution<float> nd(0.f, 1.f);
   auto init = [&](int off, int rows, int cols) {
-    const float sc = std::sqrt(2.f / (float)cols);
+    const float sc = std::sqrt(1.f / (float)cols);
     for (int i = 0; i < rows * cols; ++i) p[off + i] = nd(rng) * sc * mask[off + i];
   };
   init(L.oW1, WH, D);

@@ -78,15 +78,26 @@ def test_trained_warp_reduces_variance_without_bias(device):
 
 
 def test_warp_dropped_where_plain_qmc_is_better(device):
-    """Early inch step of the eg model: |f| is nearly flat, plain Sobol wins, no warp is kept."""
+    """eg model (n_tau = 256) at inch step 200, order 3 with 5 points after t_w: the fitted warp
+    has a far larger variance than plain Sobol, so fit_group_warp drops it; at an early step
+    (|f| nearly flat) the warp gains little, and a caller asking for a real gain (min_gain) gets
+    plain qMC."""
+    exp = models.eg_discrete_bath(n_tau=256)
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    gid = device.create_group(_lib.QIW_GROUP_BOLD, 3, 5, get_topologies_at_order(3, 5))
+    fit = qwarp.fit_group_warp(device, Work(gid, g.tau(0), g.tau(200), g.tau(201), 0, 0, 0))
+    assert fit.bias_sigma <= 4
+    assert fit.gain < 1 and fit.warp_id is None
     exp = models.eg_discrete_bath(n_tau=64)
     g = exp.grid
     device.set_problem(exp)
     device.set_ppgf(exp.P)
     gid = device.create_group(_lib.QIW_GROUP_BOLD, 2, 2, get_topologies_at_order(2, 2))
-    fit = qwarp.fit_group_warp(device, Work(gid, g.tau(0), g.tau(16), g.tau(17), 0, 0, 0))
+    fit = qwarp.fit_group_warp(device, Work(gid, g.tau(0), g.tau(16), g.tau(17), 0, 0, 0), min_gain=3.0)
     assert fit.bias_sigma <= 4
-    assert fit.gain < 1 and fit.warp_id is None
+    assert fit.gain < 3.0 and fit.warp_id is None
 
 
 def test_inchworm_with_warp_policy_is_unbiased(device):

@@ -52,9 +52,9 @@ def unpack(p, D):
 def forward(p, X):
     W1, b1, W2, b2, W3, b3, W4, b4 = unpack(p, X.shape[1])
     x = 2 * X - 1
-    a1 = x @ W1.T + b1; h1 = np.maximum(a1, 0)
-    a2 = h1 @ W2.T + b2; h2 = np.maximum(a2, 0)
-    a3 = h2 @ W3.T + b3; h3 = np.maximum(a3, 0)
+    a1 = x @ W1.T + b1; h1 = np.tanh(a1)
+    a2 = h1 @ W2.T + b2; h2 = np.tanh(a2)
+    a3 = h2 @ W3.T + b3; h3 = np.tanh(a3)
     lg = h3 @ W4.T + b4
     return x, h1, h2, h3, lg
 
@@ -96,11 +96,11 @@ def loss_grad(p, X, w):
     g = np.zeros_like(p)
     L = Layout(D)
     g[L.oW4:L.ob4] = (dl.T @ h3).ravel(); g[L.ob4:] = dl.sum(0)
-    d3 = (dl @ W4) * (h3 > 0)
+    d3 = (dl @ W4) * (1 - h3 * h3)
     g[L.oW3:L.ob3] = (d3.T @ h2).ravel(); g[L.ob3:L.oW4] = d3.sum(0)
-    d2 = (d3 @ W3) * (h2 > 0)
+    d2 = (d3 @ W3) * (1 - h2 * h2)
     g[L.oW2:L.ob2] = (d2.T @ h1).ravel(); g[L.ob2:L.oW3] = d2.sum(0)
-    d1 = (d2 @ W2) * (h1 > 0)
+    d1 = (d2 @ W2) * (1 - h1 * h1)
     g[L.oW1:L.ob1] = (d1.T @ x).ravel(); g[L.ob1:L.oW2] = d1.sum(0)
     return loss, g
 
