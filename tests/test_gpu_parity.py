@@ -358,3 +358,23 @@ def test_plan_cache_reuses_plans_across_problems(device):
     assert i4["entries"] == i3["entries"] and i4["hits"] > i3["hits"]
     for s in range(len(h.P)):
         assert np.abs(h.P[s].data - d.P[s].data).max() <= 1e-12 * np.abs(h.P[s].data).max()
+
+
+@pytest.mark.parametrize("kind,order,npa", [
+    (_lib.QIW_GROUP_BOLD, 5, 1), (_lib.QIW_GROUP_BOLD, 5, 9), (_lib.QIW_GROUP_BOLD, 6, 1),
+    (_lib.QIW_GROUP_BOLD, 6, 6), (_lib.QIW_GROUP_BARE, 5, 0), (_lib.QIW_GROUP_BARE, 6, 0),
+])
+def test_highest_orders_match_oracle(device, kind, order, npa):
+    """Orders 5 and 6 (D = 10 and 12 Sobol dimensions, the largest the batched solves use; up to
+    10395 bare topologies), FP64 and FP32, against the oracle."""
+    exp = models.anderson(n_tau=30)
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    tops = _tops(kind, order, npa)
+    gid = device.create_group(kind, order, npa, tops)
+    t = (g.tau(0), 0.0, g.tau(1)) if kind == _lib.QIW_GROUP_BARE else (g.tau(0), g.tau(20), g.tau(21))
+    N = 32
+    want = orc.OracleProblem(exp).integrate(_okind(kind), order, npa, [(x.pairs, x.parity) for x in tops], *t, N)
+    assert _rel(device.integrate([Work(gid, *t, 0, N, N)])[0], want) < REL64
+    assert _rel(device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32)[0], want) < REL32

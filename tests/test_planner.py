@@ -34,6 +34,7 @@ def _case(exp, kind, order, npa, times, N, budget=8192, corr=None):
     (_lib.QIW_GROUP_BARE, 1, 0), (_lib.QIW_GROUP_BARE, 3, 0),
     (_lib.QIW_GROUP_BOLD, 0, 0), (_lib.QIW_GROUP_BOLD, 1, 1), (_lib.QIW_GROUP_BOLD, 2, 3),
     (_lib.QIW_GROUP_BOLD, 3, 3), (_lib.QIW_GROUP_BOLD, 4, 1), (_lib.QIW_GROUP_BOLD, 4, 7),
+    (_lib.QIW_GROUP_BOLD, 5, 1), (_lib.QIW_GROUP_BOLD, 5, 9), (_lib.QIW_GROUP_BARE, 5, 0),
 ])
 def test_anderson_groups(kind, order, npa):
     exp = models.anderson(n_tau=30)
