@@ -85,6 +85,22 @@ def test_budget_split_gives_same_result():
     assert hp_b.arena <= budget < hp_a.arena
 
 
+def test_packing_limits_are_reported():
+    """The planner packs positions and pair indices into bytes: a problem with more than 256
+    interaction pairs is refused with QIW_ERR_UNSUPPORTED instead of being planned wrongly."""
+    from qiw.expansion import Expansion
+    base = models.anderson(n_tau=8)
+    pairs = list(base.pairs) * 65   # 260 pairs
+    exp = Expansion(base.ed, base.grid, pairs)
+    pk = _lib.PackedProblem(exp)
+    with pytest.raises(_lib.QiwError) as ei:
+        pe.HostPlan(pk, _lib.QIW_GROUP_BOLD, 1, 1, get_topologies_at_order(1, 1))
+    assert ei.value.code == _lib.QIW_ERR_UNSUPPORTED
+    exp = Expansion(base.ed, base.grid, list(base.pairs) * 64)   # 256 pairs: planned
+    assert pe.HostPlan(_lib.PackedProblem(exp), _lib.QIW_GROUP_BOLD, 1, 1,
+                       get_topologies_at_order(1, 1)).batches > 0
+
+
 def test_offdiagonal_leaf_is_reported():
     """A block off-diagonal leaf raises, like the reference's assertion (topology_eval.jl:462)."""
     from qiw import operators as op
