@@ -264,6 +264,16 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
       }
       break;
     }
+    case OP_PMAXPY: {  // PMUL then AXPY, the same roundings
+      const T x = A[I.a] * A[I.src];
+      if (I.w < 0 && !has_c(I)) {
+        A[I.dst] = I.acc ? x + A[I.dst] : x;
+      } else {
+        const T coef = edge_coef<T>(I, A);
+        A[I.dst] = I.acc ? fmaT<T>(coef, x, A[I.dst]) : coef * x;
+      }
+      break;
+    }
     case OP_LEAF:
       R[I.a] += (double)A[I.src];
       break;

@@ -20,6 +20,7 @@ enum Opcode : uint8_t {
   OP_AXPY = 6,    // dst (=|+=) c*w * src    (rows*cols elements)
   OP_LEAF = 7,    // R[a ...] += src         (rows*cols elements)
   OP_LOADI = 8,   // dst[rows x rows] = c * identity      (root before a zero-length interval)
+  OP_PMAXPY = 9,  // 1x1 programs only: dst (=|+=) c*w * (Pm[a] * src)  (a P multiply fused into its one AXPY)
 };
 
 struct alignas(16) Instr {     // 32 bytes

@@ -310,6 +310,8 @@ struct Builder {
     return v.real();
   }
 
+  bool diagP_group() const { return g.kind == QIW_GROUP_BARE; }
+
   // Schedule one batch into instructions; dynamic offsets relative to dyn_base.
   int schedule(std::vector<DNode> &nodes, std::vector<DEdge> &edges, std::vector<Instr> &ins,
                int64_t *peak, double *flops, const std::vector<int> &res_off) {
@@ -325,6 +327,8 @@ struct Builder {
     for (int i = N - 1; i >= 0; --i)
       if (nodes[i].alive && nodes[i].pos == 0) stack.push_back(i);
     const int last = L.n - 1;
+    bool all_scalar = opt.fuse_scalar;
+    for (int t = 0; t < pb.S; ++t) all_scalar = all_scalar && pb.dims[t] == 1;
     double fl = 0.0;
     auto mk = [](uint8_t op) { Instr I; std::memset(&I, 0, sizeof(I)); I.op = op; I.w = -1; I.c = 1.0; return I; };
     std::vector<int> ready;
@@ -349,6 +353,49 @@ struct Builder {
       const bool zero_iv = !L.zero_iv.empty() && L.zero_iv[nu.pos];
       const bool ident_root = nu.root_top >= 0 && nu.root_op < 0;
       int pmj = zero_iv ? -1 : pmid(nu.pos, nu.s);
+      // 1x1 problems: a P multiply whose one live out-edge is an AXPY (not the alias case, where
+      // the product already is V_v) becomes one PMAXPY; the product is rounded as before.
+      if (all_scalar && !zero_iv && !ident_root && n_out_alive[u] == 1) {
+        int fe = -1;
+        for (int e : nu.out)
+          if (nodes[edges[e].v].alive) { fe = e; break; }
+        const DEdge &E = edges[fe];
+        const int v = E.v;
+        const bool alias = E.op < 0 && E.w < 0 && pending[v] == 1 && slot[v] < 0;
+        bool ok = E.op < 0;
+        double sc = 1.0;
+        if (!ok && opt.fold_scalar_ops) sc = op_scalar(E.op, nu.s, &ok);
+        if (!alias && ok) {
+          int64_t src = slot[u];
+          if (nu.root_top >= 0) {  // operator root: materialise parity * O_B
+            src = al.alloc(1);
+            Instr I = mk(OP_LOADC);
+            I.rows = 1;
+            I.cols = 1;
+            I.dst = (int32_t)src;
+            I.a = (int32_t)pb.op_valoff[(size_t)nu.root_op * pb.S + nu.s0];
+            I.c = nu.root_c;
+            ins.push_back(I);
+          }
+          al.release(src, 1);
+          const bool acc = slot[v] >= 0;
+          if (!acc) slot[v] = al.alloc(1);
+          Instr I = mk(OP_PMAXPY);
+          I.rows = 1;
+          I.inner = 1;
+          I.cols = 1;
+          I.acc = acc;
+          I.dst = (int32_t)slot[v];
+          I.src = (int32_t)src;
+          I.a = pmj;
+          I.w = E.w;
+          I.c = (E.op < 0) ? 1.0 : sc;
+          ins.push_back(I);
+          fl += (diagP_group() ? 1.0 : 2.0) + ((E.w >= 0 || I.c != 1.0 ? 1 : 0) + (acc ? 1 : 0));
+          if (--pending[v] == 0) stack.push_back(v);
+          continue;
+        }
+      }
       int64_t tmp = (zero_iv && !ident_root) ? -1 : al.alloc((int64_t)d * d0);
       bool diagP = (g.kind == QIW_GROUP_BARE);
       if (ident_root && zero_iv) {
@@ -774,7 +821,8 @@ int plan_group(const HostProblem &pb, const GroupSpec &g, const PlanOptions &opt
     switch (I.op) {
       case OP_LOADP: I.a = pm_off[I.a]; I.dst += (int32_t)dyn_base; break;
       case OP_PMUL:
-      case OP_PMULD: I.a = pm_off[I.a]; I.dst += (int32_t)dyn_base; I.src += (int32_t)dyn_base; break;
+      case OP_PMULD:
+      case OP_PMAXPY: I.a = pm_off[I.a]; I.dst += (int32_t)dyn_base; I.src += (int32_t)dyn_base; break;
       case OP_LOADC:
       case OP_LOADI: I.dst += (int32_t)dyn_base; break;
       case OP_OMUL:

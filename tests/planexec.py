@@ -180,6 +180,9 @@ def execute(plan: HostPlan, exp, packed, P_tables, t_i, t_w, t_f, N, first=0, m=
             A[dst:dst + rows * cols] = (A[dst:dst + rows * cols] if accf else 0.0) + coef * A[src:src + rows * cols]
         elif op == 7:
             R[a:a + rows * cols] += A[src:src + rows * cols]
+        elif op == 9:   # 1x1 P multiply fused into its AXPY
+            coef = c * (A[w] if w >= 0 else 1.0)
+            A[dst] = (A[dst] if accf else 0.0) + coef * (A[a] * A[src])
         elif op == 8:
             A[dst:dst + rows * rows] = 0.0
             for r in range(rows):
