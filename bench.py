@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy", "batch", "warp", "correlators"])
     ap.add_argument("--step", type=int, default=200, help="warp mode: inch step (tau_w index) the warps are fitted at")
+    ap.add_argument("--warp-groups-only", action="store_true",
+                    help="warp mode: per-group fits only (no 2^20-sample step reference; for t2g)")
     ap.add_argument("--solves", type=int, default=64, help="batch mode: independent Anderson solves")
     ap.add_argument("--seed", type=int, default=2024, help="batch mode: parameter seed (numpy PCG64)")
     ap.add_argument("--no-sequential", action="store_true", help="batch mode: skip the one-solve-at-a-time arm")
@@ -452,6 +454,11 @@ def run_warp(args):
             rows.append({"order": o, "n_pts_after": npa, "topologies": len(tops), "variance_gain": fit.gain,
                          "kept": fit.warp_id is not None, "bias_sigma": fit.bias_sigma, "loss": fit.loss,
                          "fit_s": time.perf_counter() - t0})
+    if args.warp_groups_only:
+        print(json.dumps({"mode": "warp", "config": {"workload": desc + f", inch step tau_w index {n}",
+                                                      "train_samples": 2 ** 16, "replicas": 16, "N_per_replica": 1024},
+                          "groups": rows}))
+        return
     # the whole step: every group summed, plain vs warped (kept warps), against plain at 2^20
     fits = {}
     gids = []
