@@ -40,3 +40,13 @@ def test_null_arguments_are_rejected():
     assert lib.qiw_batch_add(None, None, None) == _lib.QIW_ERR_ARG
     assert lib.qiw_batch_run(None, 0, 0, None, 0) == _lib.QIW_ERR_ARG
     assert lib.qiw_batch_last_error(None) == b"null batch"
+
+
+def test_plan_cache_calls_need_no_device():
+    """qiw_plan_cache_info / qiw_plan_cache_clear touch host memory only."""
+    lib = _lib.load()
+    assert lib.qiw_plan_cache_clear() == _lib.QIW_OK
+    e, h, b = C.c_int64(-1), C.c_int64(-1), C.c_int64(-1)
+    assert lib.qiw_plan_cache_info(C.byref(e), C.byref(h), C.byref(b)) == _lib.QIW_OK
+    assert e.value == 0 and b.value == 0 and h.value >= 0
+    assert lib.qiw_plan_cache_info(None, None, None) == _lib.QIW_OK
