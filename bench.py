@@ -41,7 +41,8 @@ UNIT = "topology-samples/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 8; batch mode: 1, a step there is the whole multi-solve run)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--samples", type=int, default=1024)
@@ -634,6 +635,8 @@ def run_batch(args):
 
 if __name__ == "__main__":
     a = parse()
+    if a.steps is None:
+        a.steps = 1 if (a.mode == "batch" and a.impl != "reference") else 8
     if a.impl == "reference":
         run_reference(a)
     elif a.mode == "accuracy":
