@@ -44,7 +44,7 @@ struct DNode {
   int root_top = -1;             // >= 0: root of topology root_top (value parity * I or * O_B)
   int root_op = -1;
   double root_c = 1.0;
-  std::vector<int> out;
+  int out_begin = 0, out_count = 0;  // out-edges: edges[out_begin .. out_begin + out_count)
   int n_in = 0;
   bool alive = false;
 };
@@ -228,10 +228,11 @@ struct Builder {
       std::vector<int> next;
       for (int u : layer) {
         const State cur = states[u];
+        nodes[u].out_begin = (int)edges.size();  // a state's out-edges are appended together
         auto add_edge = [&](const State &st, int op, int w) {
           int v = get(pos, st);
           edges.push_back(DEdge{u, v, op, w});
-          nodes[u].out.push_back((int)edges.size() - 1);
+          nodes[u].out_count++;
           nodes[v].n_in++;
           if (nodes[v].n_in == 1) next.push_back(v);
         };
@@ -294,7 +295,7 @@ struct Builder {
     // Backward liveness.
     for (int i = (int)nodes.size() - 1; i >= 0; --i) {
       if (nodes[i].alive) continue;
-      for (int e : nodes[i].out)
+      for (int e = nodes[i].out_begin; e < nodes[i].out_begin + nodes[i].out_count; ++e)
         if (nodes[edges[e].v].alive) { nodes[i].alive = true; break; }
     }
     return 0;
@@ -357,7 +358,7 @@ struct Builder {
       // the product already is V_v) becomes one PMAXPY; the product is rounded as before.
       if (all_scalar && !zero_iv && !ident_root && n_out_alive[u] == 1) {
         int fe = -1;
-        for (int e : nu.out)
+        for (int e = nu.out_begin; e < nu.out_begin + nu.out_count; ++e)
           if (nodes[edges[e].v].alive) { fe = e; break; }
         const DEdge &E = edges[fe];
         const int v = E.v;
@@ -444,7 +445,7 @@ struct Builder {
       }
       bool tmp_taken = false;
       ready.clear();
-      for (int e : nu.out) {
+      for (int e = nu.out_begin; e < nu.out_begin + nu.out_count; ++e) {
         const DEdge &E = edges[e];
         if (!nodes[E.v].alive) continue;
         int v = E.v;
