@@ -35,7 +35,7 @@ class OracleDevice:
 
     def create_group(self, kind, order, n_pts_after, tops, corr=None):
         gid = len(self.groups)
-        okind = {0: "bold", 1: "bare", 2: "corr"}[kind]
+        okind = {0: "bold", 1: "bare", 2: "corr", 3: "sigma"}[kind]
         self.groups[gid] = (okind, order, n_pts_after, [(t.pairs, t.parity) for t in tops], corr)
         self.group_info[gid] = (kind, order, n_pts_after)
         return gid
@@ -70,6 +70,67 @@ def _worker(rank, world, port, q):
     inchworm(exp, range(0, 3), range(0, 3), 32, dev=OracleDevice(), comm=TorchComm())
     q.put((rank, [P_s.data.copy() for P_s in exp.P]))
     dist.destroy_process_group()
+
+
+def _worker_corr_diff(rank, world, port, q):
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for p in (os.path.join(root, "qinchworm.jl_gb300"), os.path.join(root, "oracle"), os.path.join(root, "tests")):
+        sys.path.insert(0, p)
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from qiw import models
+    from qiw.inchworm import correlator_2p, diff_inchworm, TorchComm
+    from test_multirank import OracleDevice
+    exp = models.anderson(n_tau=8, corr=True)
+    G = correlator_2p(exp, range(0, 3), 32, dev=OracleDevice(), comm=TorchComm())
+    exp_d = models.anderson(n_tau=8)
+    diff_inchworm(exp_d, range(0, 3), 32, dev=OracleDevice(), comm=TorchComm())
+    q.put((rank, ([np.asarray(g) for g in G], [P_s.data.copy() for P_s in exp_d.P])))
+    dist.destroy_process_group()
+
+
+def _run_ranks(target, world=2):
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=target, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    import queue
+    import time
+    res = {}
+    deadline = time.time() + 900
+    while len(res) < len(procs) and time.time() < deadline:
+        try:
+            r, v = q.get(timeout=5)
+            res[r] = v
+        except queue.Empty:
+            if any(p.exitcode not in (None, 0) for p in procs):
+                break
+    for p in procs:
+        p.join(timeout=300)
+        assert p.exitcode == 0
+    assert sorted(res) == list(range(world))
+    return res
+
+
+def test_two_rank_correlator_and_diff_inchworm_equal_single_rank():
+    """correlator_2p (src/inchworm.jl:868-889) and diff_inchworm! (:573-594) split their samples
+    over ranks the same way; two gloo ranks reproduce the single-rank oracle."""
+    import oracle as orc
+    from qiw import models
+    res = _run_ranks(_worker_corr_diff)
+    exp = models.anderson(n_tau=8, corr=True)
+    want_G = orc.correlator_2p(orc.OracleProblem(exp), range(0, 3), 32)
+    pb, _ = orc.diff_inchworm(models.anderson(n_tau=8), range(0, 3), 32)
+    for r in (0, 1):
+        G, P = res[r]
+        for a, b in zip(G, want_G):
+            assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
+        for s in range(len(pb.P_data)):
+            assert np.abs(P[s] - pb.P_data[s]).max() <= 1e-13 * np.abs(pb.P_data[s]).max()
 
 
 def test_two_rank_inchworm_equals_single_rank():
