@@ -17,7 +17,7 @@ import ctypes as C
 import math
 import os
 import subprocess
-from typing import Dict, List, Optional, Sequence
+from typing import Callable, Dict, List, Optional, Sequence
 
 import numpy as np
 
@@ -452,3 +452,20 @@ def correlator_2p(pb: OracleProblem, orders, N_samples: int, n_ranks: int = 1,
             g[q] = val / Z
         out.append(g)
     return out
+
+
+def mean_std_from_randomization(f: Callable, new_seq: Callable, N_seqs: int, target_std: float):
+    """mean_std_from_randomization restated (src/randomization.jl:86-100).
+
+    new_seq() plays the sequence constructor seq_type(D; scramble_rng): every call makes (and,
+    scrambled, draws) the next sequence (m, x0); f(m, x0) is the quantity of one sequence.  The
+    loop stops after sequence s > 1 once norm(std(samples), Inf) <= target_std; std is Julia's
+    corrected std (NaN for one sample)."""
+    samples = []
+    for s in range(1, N_seqs + 1):
+        m, x0 = new_seq()
+        samples.append(np.atleast_1d(np.asarray(f(m, x0), dtype=np.complex128)).ravel())
+        if s > 1 and np.max(np.std(np.array(samples), axis=0, ddof=1)) <= target_std:
+            break
+    a = np.array(samples)
+    return a.mean(axis=0), (a.std(axis=0, ddof=1) if len(a) > 1 else np.full(a.shape[1], np.nan))

@@ -11,6 +11,7 @@ normalize! and the (optional) rank decomposition and all-reduce.
 """
 from __future__ import annotations
 
+import copy
 import math
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence, Tuple
@@ -91,6 +92,81 @@ def _unpack_blocks(v: np.ndarray, dims) -> List[np.ndarray]:
     return out
 
 
+def _rng_state(rng):
+    return copy.deepcopy(rng.__dict__)
+
+
+def _rng_set(rng, state) -> None:
+    rng.__dict__.clear()
+    rng.__dict__.update(copy.deepcopy(state))
+
+
+def _mean_std(vs: np.ndarray):
+    std = vs.std(axis=0, ddof=1) if len(vs) > 1 else np.full(vs.shape[1], np.nan)
+    return vs.mean(axis=0), std
+
+
+def _randomized(groups, sobol, launch, stat):
+    """mean_std_from_randomization (src/randomization.jl:86-100) for every group of one call,
+    with the reference's draws: groups in order, group g draws the scramble of sequence s only
+    when it evaluates it, and stops after s > 1 once the largest |std(samples[1:s])| is at most
+    target_std.  Unscrambled sequences are all the same sequence: one evaluation, std 0 (NaN for
+    N_seqs = 1, as Julia's std of one sample).
+
+    groups[i] is None or (D, RandomizationParams); launch(items), items a list of (i, [(m, x0),
+    ...]) (m None for D = 0), returns {i: [all-reduced packed value per sequence]} from one
+    qiw_integrate call; stat(i, v) is the quantity the statistics apply to.  Every sequence of
+    every pending group runs in one launch; when a group stops early, the scrambling generators
+    are set back to where the reference leaves them and the later groups are drawn and run
+    again.  Returns per group (mean, std) of stat."""
+    out = [None] * len(groups)
+    todo = [i for i, g in enumerate(groups) if g is not None]
+    while todo:
+        items, snaps = [], {}
+        for i in todo:
+            D, rp = groups[i]
+            if D == 0 or rp.rng is None:
+                items.append((i, [(sobol(D), np.zeros(D, np.uint32)) if D else (None, None)]))
+                continue
+            pre, post, seqs = _rng_state(rp.rng), [], []
+            for _ in range(rp.N_seqs):
+                seqs.append(scramble(sobol(D), rp.rng))
+                post.append(_rng_state(rp.rng))
+            snaps[i] = (pre, post)
+            items.append((i, seqs))
+        vals = launch(items)
+        restart = None
+        for pos, i in enumerate(todo):
+            D, rp = groups[i]
+            vs = np.array([stat(i, v) for v in vals[i]])
+            if D == 0 or rp.rng is None:
+                n = 1 if D == 0 else rp.N_seqs
+                out[i] = (vs[0], np.full(vs.shape[1], np.nan) if n == 1 else np.zeros(vs.shape[1]))
+                continue
+            k = len(vs)
+            for s_ in range(2, len(vs) + 1):
+                if np.max(vs[:s_].std(axis=0, ddof=1)) <= rp.target_std:
+                    k = s_
+                    break
+            out[i] = _mean_std(vs[:k])
+            if k < len(vs):
+                restart = (pos, i, k)
+                break
+        if restart is None:
+            break
+        pos, i, k = restart
+        rng = groups[i][1].rng
+        _rng_set(rng, snaps[i][1][k - 1])
+        todo = todo[pos + 1:]
+        seen = {id(rng)}
+        for j in todo:   # other generators: back to their state before this round's later draws
+            Dj, rpj = groups[j]
+            if j in snaps and id(rpj.rng) not in seen:
+                _rng_set(rpj.rng, snaps[j][0])
+                seen.add(id(rpj.rng))
+    return out
+
+
 class _Session:
     """Per-run state: device, problem upload and planned groups."""
 
@@ -117,59 +193,43 @@ class _Session:
         """All groups of a step; returns per group (mean blocks, std blocks or None).  `warps`
         maps a group id to a learned warp its samples are drawn through."""
         dims = self.exp.dims
-        plan = []
+        entries = []
         for td in tds:
             D = 2 * td.order - (2 if kind == _lib.QIW_GROUP_SIGMA else 0)   # integrated times
             if D > 0 and td.N_samples <= 0:
-                plan.append(None)
+                entries.append(None)
                 continue
-            gid = self.group(kind, td, corr)
-            seqs = []
-            n_seqs = 1 if D == 0 else td.rand_params.N_seqs
-            for s in range(n_seqs):
-                if D == 0 or td.rand_params.rng is None:
-                    m = self.dev.sobol(D) if D else None
-                    x0 = np.zeros(D, np.uint32) if D else None
-                else:
-                    m, x0 = scramble(self.dev.sobol(D), td.rand_params.rng)
-                seqs.append((m, x0))
-            plan.append((gid, td, seqs))
-        # one launch for every (group, sequence) of the step
-        works, index = [], []
-        for gi, p in enumerate(plan):
-            if p is None:
-                continue
-            gid, td, seqs = p
-            exact = seqs[0][0] is None   # nothing to integrate: every rank evaluates it once
-            start, length = (0, 1) if exact else rank_sub_range(td.N_samples, comm)
-            for si, (m, x0) in enumerate(seqs):
-                works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
-                index.append((gi, si))
-        wl = [warps.get(w.group, -1) for w in works] if warps else None
-        if wl is not None and all(x < 0 for x in wl):
-            wl = None
-        if not works:
-            res = []
-        elif wl is None:
-            res = self.dev.integrate(works, precision)
-        else:
-            res = self.dev.integrate(works, precision, warps=wl)
-        per: Dict[int, List[np.ndarray]] = {}
-        for (gi, si), blocks in zip(index, res):
-            v = _pack_blocks(blocks)
-            if plan[gi][2][0][0] is not None:
-                v = comm.allreduce(v)
-            per.setdefault(gi, []).append(v)
-        out = []
-        for gi, p in enumerate(plan):
-            if p is None:
-                out.append(None)
-                continue
-            vs = np.array(per[gi])
-            mean = vs.mean(axis=0)
-            std = vs.std(axis=0, ddof=1) if len(vs) > 1 else np.full(vs.shape[1], np.nan)
-            out.append((_unpack_blocks(mean, dims), _unpack_blocks(std, dims)))
-        return out
+            entries.append((self.group(kind, td, corr), td, D))
+
+        def launch(items):
+            # one launch for every (group, sequence) of the step
+            works, index = [], []
+            for i, seqs in items:
+                gid, td, D = entries[i]
+                start, length = (0, 1) if D == 0 else rank_sub_range(td.N_samples, comm)  # exact: once per rank
+                for m, x0 in seqs:
+                    works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
+                    index.append(i)
+            wl = [warps.get(w.group, -1) for w in works] if warps else None
+            if wl is not None and all(x < 0 for x in wl):
+                wl = None
+            if not works:
+                res = []
+            elif wl is None:
+                res = self.dev.integrate(works, precision)
+            else:
+                res = self.dev.integrate(works, precision, warps=wl)
+            vals: Dict[int, List[np.ndarray]] = {}
+            for i, blocks in zip(index, res):
+                v = _pack_blocks(blocks)
+                if entries[i][2] > 0:
+                    v = comm.allreduce(v)
+                vals.setdefault(i, []).append(v)
+            return vals
+
+        stats = _randomized([None if e is None else (e[2], e[1].rand_params) for e in entries],
+                            self.dev.sobol, launch, lambda i, v: v)
+        return [None if r is None else (_unpack_blocks(r[0], dims), _unpack_blocks(r[1], dims)) for r in stats]
 
 
 def inchworm_step(expansion, t_i: float, t_w: float, t_f: float, top_data: Sequence[TopologiesInputData],
@@ -382,10 +442,10 @@ def correlator_2p(expansion, orders, N_samples: int, rand_params: Optional[Rando
     stds = [np.zeros(len(idx)) for _ in range(n_c)]
     for (q, j, a, n), c, r in zip(spans, corrs, works_res):
         val, sd = 0j, 0.0
-        for (mean, std), td in r:
-            val += sum(np.trace(b) for b in mean)
+        for mean, std, td in r:   # result += order_contrib, result_std += order_contrib_std
+            val += mean
             if td.order > 0:
-                sd += float(np.real(sum(np.trace(b) for b in std)))
+                sd += std
         gs[c][q] = val / Z
         stds[c][q] = sd / Z.real
     return (gs, stds) if request_std else gs
@@ -393,41 +453,39 @@ def correlator_2p(expansion, orders, N_samples: int, rand_params: Optional[Rando
 
 def _run_multi_tau(ses: _Session, all_tds, spans, times, precision, comm, corrs):
     """Runs the correlator groups of every span (correlator corrs[i], one tau point) in one
-    qiw_integrate call."""
-    dims = ses.exp.dims
-    works, index = [], []
-    for si, ((q, j, a, n), (t_i, t_w, t_f)) in enumerate(zip(spans, times)):
+    qiw_integrate call.  The randomized quantity is the trace of the group's result, as in the
+    reference's tr(eval(...)) integrand (src/inchworm.jl:861-879).  Returns per span a list of
+    (mean trace, std of the trace, TopologiesInputData)."""
+    entries = []   # (span, td index, gid, D) in the reference's order: correlator, tau, group
+    for si, (q, j, a, n) in enumerate(spans):
         for k in range(n):
             td = all_tds[a + k]
             if td.order > 0 and td.N_samples <= 0:
                 continue
-            gid = ses.group(_lib.QIW_GROUP_CORRELATOR, td, corrs[si])
-            D = 2 * td.order
-            n_seqs = 1 if td.order == 0 else td.rand_params.N_seqs
-            for s in range(n_seqs):
-                if D == 0 or td.rand_params.rng is None:
-                    m, x0 = (ses.dev.sobol(D), np.zeros(D, np.uint32)) if D else (None, None)
-                else:
-                    m, x0 = scramble(ses.dev.sobol(D), td.rand_params.rng)
-                start, length = rank_sub_range(td.N_samples, comm) if td.order > 0 else (0, 1)
+            entries.append((si, a + k, ses.group(_lib.QIW_GROUP_CORRELATOR, td, corrs[si]), 2 * td.order))
+
+    def launch(items):
+        works, index = [], []
+        for i, seqs in items:
+            si, ti, gid, D = entries[i]
+            td = all_tds[ti]
+            t_i, t_w, t_f = times[si]
+            start, length = rank_sub_range(td.N_samples, comm) if D > 0 else (0, 1)
+            for m, x0 in seqs:
                 works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
-                index.append((si, a + k))
-    res = ses.dev.integrate(works, precision) if works else []
-    grouped: Dict[Tuple[int, int], List[np.ndarray]] = {}
-    for (si, ti), blocks in zip(index, res):
-        v = _pack_blocks(blocks)
-        if all_tds[ti].order > 0:
-            v = comm.allreduce(v)
-        grouped.setdefault((si, ti), []).append(v)
-    out = []
-    for si, (q, j, a, n) in enumerate(spans):
-        r = []
-        for k in range(n):
-            vs = np.array(grouped.get((si, a + k), []))
-            if len(vs) == 0:
-                continue
-            mean = vs.mean(axis=0)
-            std = vs.std(axis=0, ddof=1) if len(vs) > 1 else np.full(vs.shape[1], np.nan)
-            r.append(((_unpack_blocks(mean, dims), _unpack_blocks(std, dims)), all_tds[a + k]))
-        out.append(r)
+                index.append(i)
+        res = ses.dev.integrate(works, precision) if works else []
+        vals: Dict[int, List[np.ndarray]] = {}
+        for i, blocks in zip(index, res):
+            v = np.array([sum(np.trace(b) for b in blocks)], np.complex128)
+            if entries[i][3] > 0:
+                v = comm.allreduce(v)
+            vals.setdefault(i, []).append(v)
+        return vals
+
+    stats = _randomized([(e[3], all_tds[e[1]].rand_params) for e in entries], ses.dev.sobol, launch,
+                        lambda i, v: v)
+    out = [[] for _ in spans]
+    for e, (mean, std) in zip(entries, stats):
+        out[e[0]].append((complex(mean[0]), float(std[0]), all_tds[e[1]]))
     return out
