@@ -3,6 +3,7 @@
 Reads (never executes) the reference repository:
   * test/inchworm.h5           /inchworm/P/{1,2}, /inchworm/g   (written by test/inchworm.jl:180-212),
                                 /diff_inchworm/P/{1,2}           (test/inchworm.jl:214-239)
+  * test/topology_eval.h5      /x1_list, /xs_list, /values       (test/topology_eval.jl:53-140)
   * test/scrambled_sobol.jl    MockRNG-scrambled Sobol vectors   (test/scrambled_sobol.jl:136-179)
   * README.md                  Z and rho of the README Anderson run (README.md:203-204)
 and writes small JSON files that the tests use on machines without the reference.
@@ -40,6 +41,23 @@ def inchworm_h5(ref: str):
         "diff_P": [_cplx(f.read(f"/diff_inchworm/P/{s}")) for s in (1, 2)],
     }
     with open(os.path.join(HERE, "inchworm_h5.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+
+
+def topology_eval_h5(ref: str):
+    """TopologyEvaluator values of the order-3, n_pts_after = 1 topologies of the single-level
+    model at 100 explicit time sets (test/topology_eval.jl:53-140)."""
+    f = H5File(os.path.join(ref, "test", "topology_eval.h5"))
+    vals = f.read("/values")   # [100][2]: sectors 1 and 2
+    out = {
+        "source": "test/topology_eval.h5 (read by test/topology_eval.jl:95-140)",
+        "model": {"beta": 10.0, "mu": 0.1, "eps": 0.1, "V": -0.1, "n_tau": 30, "order": 3,
+                  "n_pts_after": 1, "tau_index_w": 6, "tau_index_f": 7},
+        "x1_list": [float(x) for x in f.read("/x1_list")],
+        "xs_list": [[float(x) for x in row] for row in f.read("/xs_list")],   # [5][100]
+        "values": [_cplx(vals[:, s]) for s in range(vals.shape[1])],
+    }
+    with open(os.path.join(HERE, "topology_eval_h5.json"), "w") as fh:
         json.dump(out, fh, indent=1)
 
 
@@ -88,6 +106,7 @@ def readme_output(ref: str):
 if __name__ == "__main__":
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     inchworm_h5(ref)
+    topology_eval_h5(ref)
     sobol_vectors(ref)
     readme_output(ref)
     print("fixtures written to", HERE)

@@ -121,8 +121,38 @@ def execute(plan: HostPlan, exp, packed, P_tables, t_i, t_w, t_f, N, first=0, m=
                 u[dg:] = u[dg:] * (t_w - t_i) + t_i
         for j in range(D):
             tm[plan.var_pos[j]] = u[j]
-    A = np.zeros((plan.arena, Ns))
+    R = run_program(plan, exp, packed, P_tables, tm)
+    tot = R.sum(axis=1)
+    if D > 0:
+        if plan.kind in (1, 3):
+            J = math.prod([(t_f - t_i) / i for i in range(1, D + 1)])
+        else:
+            J = math.prod([(t_w - t_i) / i for i in range(1, plan.d_before + 1)] or [1.0]) * \
+                math.prod([(t_f - t_w) / i for i in range(1, plan.d_after + 1)] or [1.0])
+        scale = J / N
+    else:
+        scale = 1.0
+    if plan.kind == 3:   # self-energy groups: +i * parity (2k - 2 integrated times)
+        scale = -scale
+    out = -1j * scale * tot
+    blocks, o = [], 0
+    for d in dims:
+        blocks.append(out[o:o + d * d].reshape(d, d, order="F"))
+        o += d * d
+    return blocks
+
+
+
+def run_program(plan: HostPlan, exp, packed, P_tables, tm: np.ndarray) -> np.ndarray:
+    """The group's program at explicit node times tm[n_nodes][Ns]: per-sample real-phase sums
+    R[res_size][Ns] (qiw_integrate returns -i * J/N * parity-signed sum over samples)."""
+    Ns = tm.shape[1]
+    dims = packed.dims
+    h = exp.grid.step
+    inv_h = 1.0 / h
+    opv = packed.op_values[0::2]
     eoff = np.concatenate([[0], np.cumsum(dims)[:-1]])
+    A = np.zeros((plan.arena, Ns))
     for job in plan.pm:
         iv, s, off = int(job["iv"]), int(job["s"]), int(job["off"])
         dt = np.maximum(tm[iv + 1] - tm[iv], 0.0)
@@ -189,24 +219,7 @@ def execute(plan: HostPlan, exp, packed, P_tables, t_i, t_w, t_f, N, first=0, m=
                 A[dst + r * rows + r] = c
         else:
             raise ValueError(f"bad opcode {op}")
-    tot = R.sum(axis=1)
-    if D > 0:
-        if plan.kind in (1, 3):
-            J = math.prod([(t_f - t_i) / i for i in range(1, D + 1)])
-        else:
-            J = math.prod([(t_w - t_i) / i for i in range(1, plan.d_before + 1)] or [1.0]) * \
-                math.prod([(t_f - t_w) / i for i in range(1, plan.d_after + 1)] or [1.0])
-        scale = J / N
-    else:
-        scale = 1.0
-    if plan.kind == 3:   # self-energy groups: +i * parity (2k - 2 integrated times)
-        scale = -scale
-    out = -1j * scale * tot
-    blocks, o = [], 0
-    for d in dims:
-        blocks.append(out[o:o + d * d].reshape(d, d, order="F"))
-        o += d * d
-    return blocks
+    return R
 
 
 def p_tables(exp):
