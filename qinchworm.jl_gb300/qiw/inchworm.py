@@ -179,13 +179,18 @@ class _Session:
             self.dev._problem_key = key
             self.dev._groups = {}
         self.exp = expansion
+        self._by_td: Dict[tuple, tuple] = {}
 
     def group(self, kind: int, td: TopologiesInputData, corr: Optional[int] = None) -> int:
+        hit = self._by_td.get((kind, id(td), corr))
+        if hit is not None and hit[0] is td:
+            return hit[1]
         key = (kind, td.order, td.n_pts_after, corr, tuple((t.pairs, t.parity) for t in td.topologies))
         g = self.dev._groups.get(key)
         if g is None:
             g = self.dev.create_group(kind, td.order, td.n_pts_after, td.topologies, corr)
             self.dev._groups[key] = g
+        self._by_td[(kind, id(td), corr)] = (td, g)   # td kept alive, so its id stays its own
         return g
 
     def run(self, kind: int, tds: Sequence[TopologiesInputData], t_i, t_w, t_f, precision, comm: Comm,
@@ -227,9 +232,9 @@ class _Session:
                 vals.setdefault(i, []).append(v)
             return vals
 
-        stats = _randomized([None if e is None else (e[2], e[1].rand_params) for e in entries],
-                            self.dev.sobol, launch, lambda i, v: v)
-        return [None if r is None else (_unpack_blocks(r[0], dims), _unpack_blocks(r[1], dims)) for r in stats]
+        # per group (mean, std) as packed vectors in sector order (see _pack_blocks)
+        return _randomized([None if e is None else (e[2], e[1].rand_params) for e in entries],
+                           self.dev.sobol, launch, lambda i, v: v)
 
 
 def inchworm_step(expansion, t_i: float, t_w: float, t_f: float, top_data: Sequence[TopologiesInputData],
@@ -250,21 +255,23 @@ def inchworm_step_bare(expansion, t_i: float, t_f: float, top_data: Sequence[Top
 
 
 def _accumulate(results, top_data, dims):
+    """Sums the groups of a step per order, then the orders (the reference's order of sums,
+    src/inchworm.jl:192-200), on packed vectors; returns SectorBlockMatrix values."""
     orders = sorted({td.order for td in top_data})
-    zero = lambda: [np.zeros((d, d), np.complex128) for d in dims]
-    contribs = {o: zero() for o in orders}
-    stds = {o: zero() for o in orders}
+    L = int(sum(int(d) * int(d) for d in dims))
+    contribs = {o: np.zeros(L, np.complex128) for o in orders}
+    stds = {o: np.zeros(L, np.complex128) for o in orders}
     for td, r in zip(top_data, results):
         if r is None:
             continue
         mean, std = r
-        contribs[td.order] = [a + b for a, b in zip(contribs[td.order], mean)]
+        contribs[td.order] = contribs[td.order] + mean
         if td.order > 0:
-            stds[td.order] = [a + b for a, b in zip(stds[td.order], std)]
-    total = zero()
+            stds[td.order] = stds[td.order] + std
+    total = np.zeros(L, np.complex128)
     for o in orders:
-        total = [a + b for a, b in zip(total, contribs[o])]
-    sbm = blocks_to_sbm
+        total = total + contribs[o]
+    sbm = lambda v: blocks_to_sbm(_unpack_blocks(v, dims))
     return sbm(total), {o: sbm(v) for o, v in contribs.items()}, {o: sbm(v) for o, v in stds.items()}
 
 
