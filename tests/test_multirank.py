@@ -91,6 +91,49 @@ def _worker_corr_diff(rank, world, port, q):
     dist.destroy_process_group()
 
 
+def _randomized_step(comm=None):
+    """One inch step with scrambled sequences and an early stop, through OracleDevice."""
+    from qiw import models, sobol
+    from qiw.diagrammatics import get_topologies_at_order
+    from qiw.inchworm import Comm, RandomizationParams, TopologiesInputData, inchworm_step
+    exp = models.anderson(n_tau=8)
+    g = exp.grid
+    rp = RandomizationParams(rng=sobol.NumpyBitRNG(5), N_seqs=5, target_std=3e-3)
+    tds = [TopologiesInputData(o, npa, get_topologies_at_order(o, npa), 32, rp)
+           for o in (1, 2) for npa in range(1, 2 * o)]
+    _, contribs, stds = inchworm_step(exp, g.tau(0), g.tau(3), g.tau(4), tds, dev=OracleDevice(),
+                                      comm=comm or Comm())
+    vec = lambda d: np.concatenate([d[o][s][1].ravel() for o in sorted(d) for s in sorted(d[o])])
+    return vec(contribs), vec(stds), int(rp.rng.g.integers(1 << 62))
+
+
+def _worker_randomized(rank, world, port, q):
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for p in (os.path.join(root, "qinchworm.jl_gb300"), os.path.join(root, "oracle"), os.path.join(root, "tests")):
+        sys.path.insert(0, p)
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from qiw.inchworm import TorchComm
+    from test_multirank import _randomized_step
+    q.put((rank, _randomized_step(TorchComm())))
+    dist.destroy_process_group()
+
+
+def test_two_rank_randomized_step_equals_single_rank():
+    """Scrambled sequences with an early stop on target_std: the stop is decided on the
+    all-reduced values (src/randomization.jl:95-96 after src/inchworm.jl:190), so both ranks use
+    the same sequences as one rank and leave the generator in the same state."""
+    res = _run_ranks(_worker_randomized)
+    mean, std, nxt = _randomized_step()
+    for r in (0, 1):
+        m, sd, n = res[r]
+        assert np.abs(m - mean).max() <= 1e-13 * np.abs(mean).max()
+        assert np.abs(sd - std).max() <= 1e-10 * np.abs(std).max()
+        assert n == nxt
+
+
 def _run_ranks(target, world=2):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
