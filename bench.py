@@ -191,7 +191,9 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": desc + f", orders 0:{kmax}, one inch step", "N_samples": args.samples},
+            "config": {"workload": desc + f", orders 0:{kmax}, one regular inch step per bench step",
+                       "N_samples": args.samples, "groups_per_step": len(tds),
+                       "topologies_per_step": sum(len(td.topologies) for td in tds)},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
