@@ -390,13 +390,15 @@ def diff_inchworm(expansion, orders, N_samples: int, rand_params: Optional[Rando
             for s, (sf, m) in value.items():
                 sigma[s][j_store] = m
         new = {}
+        w = np.ones(n + 1)
+        w[0] = w[n] = 0.5
+        if n == 0:
+            w[0] = 0.0
         for s, P_s in enumerate(expansion.P):
             P_prev = P_s.data[n]
-            conv = np.zeros_like(P_prev)
-            for j in range(0, n + 1):
-                w = 0.0 if n == 0 else (0.5 if j in (0, n) else 1.0)
-                conv = conv + w * (sigma[s][n - j] @ P_s.data[j])
-            conv = -1j * h * conv
+            # sum_j w_j Sigma(tau_n - tau_j) P(tau_j), j = 0..n, as one batched product
+            prods = np.matmul(sigma[s][n::-1], P_s.data[:n + 1])
+            conv = -1j * h * np.tensordot(w, prods, axes=(0, 0))
             new[s] = (s, P_prev + h * (conv - H[s] @ P_prev))
         _ppgf.set_ppgf(expansion.P, n + 1, new)
         for o in contribs:
