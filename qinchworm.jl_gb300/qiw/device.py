@@ -140,6 +140,15 @@ class Device:
                                                       out.ctypes.data))
         return self._unpack(out, len(works))
 
+    def integrate_packed(self, works: Sequence[Work], precision: int = _lib.QIW_PREC_FP64) -> np.ndarray:
+        """integrate() without unpacking: [n_work][sum d_s^2] complex, per work item the sector
+        blocks in sector order, each column-major."""
+        descs, keep = self._descs(works)
+        rs = int(np.sum(self.packed.dims ** 2))
+        out = np.zeros(2 * rs * len(works))
+        self._check(self.lib.qiw_integrate(self.h, len(works), descs, precision, out.ctypes.data))
+        return (out[0::2] + 1j * out[1::2]).reshape(len(works), rs)
+
     def integrate_samples(self, work: Work, precision: int = _lib.QIW_PREC_FP64):
         """One work item; returns (blocks, per-sample values [n_samples][sum d^2])."""
         descs, keep = self._descs([work])

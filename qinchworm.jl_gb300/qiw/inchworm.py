@@ -224,11 +224,14 @@ class _Session:
                 res = self.dev.integrate(works, precision)
             else:
                 res = self.dev.integrate(works, precision, warps=wl)
+            packed = [_pack_blocks(blocks) for blocks in res]
+            red = [k for k, i in enumerate(index) if entries[i][2] > 0]   # exact groups: every rank has it
+            if red and comm.size > 1:   # one all-reduce for every sampled work item of the launch
+                summed = comm.allreduce(np.stack([packed[k] for k in red]))
+                for r, k in enumerate(red):
+                    packed[k] = summed[r]
             vals: Dict[int, List[np.ndarray]] = {}
-            for i, blocks in zip(index, res):
-                v = _pack_blocks(blocks)
-                if entries[i][2] > 0:
-                    v = comm.allreduce(v)
+            for i, v in zip(index, packed):
                 vals.setdefault(i, []).append(v)
             return vals
 
@@ -465,6 +468,9 @@ def _run_multi_tau(ses: _Session, all_tds, spans, times, precision, comm, corrs)
     qiw_integrate call.  The randomized quantity is the trace of the group's result, as in the
     reference's tr(eval(...)) integrand (src/inchworm.jl:861-879).  Returns per span a list of
     (mean trace, std of the trace, TopologiesInputData)."""
+    dims = [int(d) for d in ses.exp.dims]
+    offs = np.concatenate([[0], np.cumsum([d * d for d in dims])[:-1]]).astype(int)
+    diag = np.array([o + k * d + k for o, d in zip(offs, dims) for k in range(d)], dtype=np.int64)
     entries = []   # (span, td index, gid, D) in the reference's order: correlator, tau, group
     for si, (q, j, a, n) in enumerate(spans):
         for k in range(n):
@@ -483,13 +489,19 @@ def _run_multi_tau(ses: _Session, all_tds, spans, times, precision, comm, corrs)
             for m, x0 in seqs:
                 works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
                 index.append(i)
-        res = ses.dev.integrate(works, precision) if works else []
+        if not works:
+            return {}
+        if hasattr(ses.dev, "integrate_packed"):   # traces straight from the packed result
+            tr = ses.dev.integrate_packed(works, precision)[:, diag].sum(axis=1)
+        else:
+            tr = np.array([sum(np.trace(b) for b in blocks) for blocks in ses.dev.integrate(works, precision)],
+                          np.complex128)
+        red = np.array([entries[i][3] > 0 for i in index])
+        if red.any() and comm.size > 1:   # one all-reduce for every sampled work item of the launch
+            tr[red] = comm.allreduce(np.ascontiguousarray(tr[red]))
         vals: Dict[int, List[np.ndarray]] = {}
-        for i, blocks in zip(index, res):
-            v = np.array([sum(np.trace(b) for b in blocks)], np.complex128)
-            if entries[i][3] > 0:
-                v = comm.allreduce(v)
-            vals.setdefault(i, []).append(v)
+        for i, t in zip(index, tr):
+            vals.setdefault(i, []).append(np.array([t]))
         return vals
 
     stats = _randomized([(e[3], all_tds[e[1]].rand_params) for e in entries], ses.dev.sobol, launch,
