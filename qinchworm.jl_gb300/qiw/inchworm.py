@@ -219,12 +219,13 @@ class _Session:
             if wl is not None and all(x < 0 for x in wl):
                 wl = None
             if not works:
-                res = []
+                packed = []
+            elif wl is None and hasattr(self.dev, "integrate_packed"):
+                packed = list(self.dev.integrate_packed(works, precision))
             elif wl is None:
-                res = self.dev.integrate(works, precision)
+                packed = [_pack_blocks(blocks) for blocks in self.dev.integrate(works, precision)]
             else:
-                res = self.dev.integrate(works, precision, warps=wl)
-            packed = [_pack_blocks(blocks) for blocks in res]
+                packed = [_pack_blocks(blocks) for blocks in self.dev.integrate(works, precision, warps=wl)]
             red = [k for k, i in enumerate(index) if entries[i][2] > 0]   # exact groups: every rank has it
             if red and comm.size > 1:   # one all-reduce for every sampled work item of the launch
                 summed = comm.allreduce(np.stack([packed[k] for k in red]))
