@@ -17,7 +17,7 @@ import ctypes as C
 import math
 import os
 import subprocess
-from typing import Callable, Dict, List, Optional, Sequence
+from typing import Callable, List, Optional, Sequence
 
 import numpy as np
 

@@ -8,7 +8,7 @@ block matrices of their operators, of the identity and of the correlator operato
 """
 from __future__ import annotations
 
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import List, Optional, Sequence, Tuple, Union
 
 import numpy as np

@@ -12,7 +12,6 @@ normalize! and the (optional) rank decomposition and all-reduce.
 from __future__ import annotations
 
 import copy
-import math
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence, Tuple
 
@@ -24,7 +23,7 @@ from .device import Device, Work, blocks_to_sbm
 from .diagrammatics import Topology, get_topologies_at_order
 from .ed import SectorBlockMatrix
 from .gf import ImaginaryTimeGF
-from .sobol import direction_numbers, scramble
+from .sobol import scramble
 
 
 @dataclass

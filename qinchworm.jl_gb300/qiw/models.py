@@ -8,7 +8,7 @@ that the reference checks against exact diagonalisation (`test/dimers.jl`).
 """
 from __future__ import annotations
 
-from typing import List, Optional, Sequence
+from typing import List
 
 import numpy as np
 

@@ -11,7 +11,7 @@ from qiw import _lib, models
 from qiw import warp as qwarp
 from qiw.device import Work
 from qiw.diagrammatics import get_topologies_at_order
-from qiw.sobol import NumpyBitRNG, direction_numbers, scramble
+from qiw.sobol import direction_numbers
 
 pytestmark = pytest.mark.gpu
 
