@@ -30,6 +30,8 @@ def test_ctx_create_reports_missing_device_without_crashing():
     h = C.c_void_p()
     rc = lib.qiw_ctx_create(C.byref(h), 0)
     assert rc == _lib.QIW_ERR_CUDA and not h.value
+    b = C.c_void_p()
+    assert lib.qiw_batch_create(C.byref(b), 0) == _lib.QIW_ERR_CUDA and not b.value
 
 
 def test_null_arguments_are_rejected():
