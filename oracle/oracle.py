@@ -371,8 +371,11 @@ def inchworm(exp, orders, orders_bare, N_samples: int, n_pts_after_max: Optional
     return pb
 
 
-def diff_inchworm(exp, orders, N_samples: int, n_ranks: int = 1, conv_factor: complex = -1j):
-    """diff_inchworm! restated (src/inchworm.jl:529-786); returns (OracleProblem, Sigma tables).
+def diff_inchworm(exp, orders, N_samples: int, n_ranks: int = 1, conv_factor: complex = -1j, rand=None):
+    """diff_inchworm! restated (src/inchworm.jl:529-786); returns (OracleProblem, Sigma tables),
+    and with `rand` = (new_seq, N_seqs, target_std) also the per-step std of Sigma summed over
+    orders (one packed vector per step); new_seq(D) makes (and draws) the next D-dimensional
+    scrambled sequence (m, x0), the role of ScrambledSobolSeq(D; scramble_rng).
 
     Per step n (tau_f_prev = tau_n, tau_f = tau_{n+1}): Sigma(tau_n) = sum over orders k >= 1 of
     the self-energy diagrams (topologies with n_pts_after = 1, PairNodes at tau_0 and tau_n);
@@ -380,9 +383,15 @@ def diff_inchworm(exp, orders, N_samples: int, n_ranks: int = 1, conv_factor: co
     (Keldysh's integrate; its contour measure on the imaginary branch is `conv_factor` * h);
     P(tau_{n+1}) = P(tau_n) + h (conv - H P(tau_n)) with H_s = diag(E_s + lambda) (Euler,
     Delta tau = 1im * step = h).  No normalisation.  With spline-interpolated P the stored
-    Sigma lags one grid point, as the reference's incremental-spline container does."""
+    Sigma lags one grid point, as the reference's incremental-spline container does.
+
+    Randomized (src/inchworm.jl:566-597): order 1 is evaluated exactly (no draws, std 0); order
+    k >= 2 draws 2k-dimensional scrambled sequences one at a time (mean_std_from_randomization
+    below) and the Root transform of the 2k - 2 integrated times reads the first 2k - 2
+    coordinates of each."""
     pb = OracleProblem(exp)
     grid = exp.grid
+    step_std = []
     S = pb.S
     h = grid.step
     groups = []
@@ -398,9 +407,23 @@ def diff_inchworm(exp, orders, N_samples: int, n_ranks: int = 1, conv_factor: co
         t_i, t_prev = grid.tau(0), grid.tau(n)
         P_prev = [pb.P_data[s][n].copy() for s in range(S)]
         total = [np.zeros((d, d), np.complex128) for d in pb.dims]
+        std_n = np.zeros(int(np.sum(pb.dims ** 2)))
         for (order, tops) in groups:
-            blk = pb.integrate("sigma", order, 1, tops, t_i, 0.0, t_prev, N_samples, n_ranks)
+            if rand is None or order == 1:
+                blk = pb.integrate("sigma", order, 1, tops, t_i, 0.0, t_prev, N_samples, n_ranks)
+            else:
+                new_seq, n_seqs, target = rand
+                D = 2 * order - 2
+                f = lambda m, x0, order=order, tops=tops: np.concatenate([b.ravel() for b in pb.integrate(
+                    "sigma", order, 1, tops, t_i, 0.0, t_prev, N_samples, n_ranks, m=m[:D], x0=x0[:D])])
+                mean, std = mean_std_from_randomization(f, lambda order=order: new_seq(2 * order), n_seqs, target)
+                std_n = std_n + std.real
+                blk, o = [], 0
+                for d in pb.dims:
+                    blk.append(mean[o:o + d * d].reshape(d, d))
+                    o += d * d
             total = [a + b for a, b in zip(total, blk)]
+        step_std.append(std_n)
         # set_ppgf!(Sigma, tau_i, tau_n, .): with spline-interpolated P, Sigma = zero(P) is an
         # incremental spline whose interpolant already holds the tau_0 point, so extend! stores
         # the value one grid point later (src/ppgf.jl:474-482, src/spline_gf.jl:333-336, 377-386)
@@ -420,7 +443,7 @@ def diff_inchworm(exp, orders, N_samples: int, n_ranks: int = 1, conv_factor: co
             rhs = conv - H[s] @ P_prev[s]
             new.append(P_prev[s] + h * rhs)
         pb.set_ppgf(n + 1, new)
-    return pb, sigma
+    return (pb, sigma) if rand is None else (pb, sigma, step_std)
 
 
 def correlator_2p(pb: OracleProblem, orders, N_samples: int, n_ranks: int = 1,

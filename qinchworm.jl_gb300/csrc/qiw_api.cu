@@ -57,7 +57,8 @@ namespace qiw {
 int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, double *out,
                    const int32_t *warp_ids, double *sample_out) {
   if (!c || n_work < 0 || (n_work > 0 && (!work || !out))) return QIW_ERR_ARG;
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_integrate: cudaSetDevice");
   if (n_work == 0) return QIW_OK;
   LaunchTables t;
   int rc = prepare_launch(c, n_work, work, precision, &t);
@@ -419,7 +420,8 @@ int qiw_ctx_create(qiw_ctx **out, int device) {
   if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return QIW_ERR_CUDA;
   qiw_ctx *c = new qiw_ctx();
   c->device = device;
-  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  qiw::DeviceScope dev_scope(device);
+  if (dev_scope.status != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
     delete c;
     return QIW_ERR_CUDA;
@@ -434,7 +436,7 @@ int qiw_ctx_create(qiw_ctx **out, int device) {
 
 void qiw_ctx_destroy(qiw_ctx *c) {
   if (!c) return;
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
   cudaStreamSynchronize(c->stream);
   c->clear_groups();
   destroy_warps(c);
@@ -461,7 +463,8 @@ double qiw_last_kernel_ms(const qiw_ctx *c) { return c ? c->last_ms : 0.0; }
 
 int qiw_problem_set(qiw_ctx *c, const qiw_problem_desc *d) {
   if (!c || !d) return QIW_ERR_ARG;
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_problem_set: cudaSetDevice");
   if (d->n_sectors <= 0 || !d->sector_dims || d->n_tau < 2 || !(d->beta > 0.0) || d->n_ops <= 0 ||
       !d->op_n_blocks || !d->op_blocks || !d->op_value_offset || !d->op_values || d->n_pairs < 0 ||
       (d->n_pairs > 0 && (!d->pair_ops || !d->pair_prop_kind || !d->pair_prop_data)) || !d->atomic_energies)
@@ -547,7 +550,8 @@ int qiw_problem_set(qiw_ctx *c, const qiw_problem_desc *d) {
 int qiw_ppgf_set(qiw_ctx *c, const double *P) {
   if (!c || !P) return QIW_ERR_ARG;
   if (!c->has_problem) return c->fail(QIW_ERR_ARG, "qiw_ppgf_set: no problem set");
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_ppgf_set: cudaSetDevice");
   std::vector<double> t(c->ptab_size);
   std::vector<float> tf(c->ptab_size);
   c->real_phase_P = true;
@@ -568,7 +572,8 @@ int qiw_ppgf_set(qiw_ctx *c, const double *P) {
 int qiw_group_create(qiw_ctx *c, const qiw_group_desc *d, int32_t *group_id) {
   if (!c || !d || !group_id) return QIW_ERR_ARG;
   if (!c->has_problem) return c->fail(QIW_ERR_ARG, "qiw_group_create: no problem set");
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_group_create: cudaSetDevice");
   GroupSpec gs;
   {
     std::string e;
@@ -629,7 +634,8 @@ int qiw_integrate_samples(qiw_ctx *c, const qiw_work_desc *work, int32_t precisi
 
 int qiw_measure_fma_peak(qiw_ctx *c, int32_t precision, double *tflops) {
   if (!c || !tflops) return QIW_ERR_ARG;
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_measure_fma_peak: cudaSetDevice");
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
   const int threads = 256, blocks = sms * 8, iters = 2048;

@@ -300,8 +300,8 @@ int qiw_batch_create(qiw_batch **out, int device) {
   if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return QIW_ERR_CUDA;
   qiw_batch *b = new qiw_batch();
   b->device = device;
-  cudaSetDevice(device);
-  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  qiw::DeviceScope dev_scope(device);
+  if (dev_scope.status != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
     qiw_batch_destroy(b);
     return QIW_ERR_CUDA;
@@ -312,7 +312,7 @@ int qiw_batch_create(qiw_batch **out, int device) {
 
 void qiw_batch_destroy(qiw_batch *b) {
   if (!b) return;
-  cudaSetDevice(b->device);
+  qiw::DeviceScope dev_scope(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   b->drop_graph();
   for (SolveRec *s : b->solves) {
@@ -357,7 +357,8 @@ int qiw_batch_add(qiw_batch *b, const qiw_solve_desc *d, int32_t *solve_id) {
     return QIW_ERR_ARG;
   if (d->n_samples == 0 || (d->n_samples & (d->n_samples - 1)) || d->n_samples > (1ull << 32))
     return b->fail(QIW_ERR_ARG, "qiw_batch_add: n_samples must be a power of 2 <= 2^32");
-  cudaSetDevice(b->device);
+  qiw::DeviceScope dev_scope(b->device);
+  if (dev_scope.status != cudaSuccess) return b->fail(QIW_ERR_CUDA, std::string("qiw_batch_add: cudaSetDevice: ") + cudaGetErrorString(dev_scope.status));
   SolveRec *s = new SolveRec();
   int rc = qiw_ctx_create(&s->ctx, b->device);
   if (rc) {
@@ -432,7 +433,8 @@ int qiw_batch_run(qiw_batch *b, int32_t precision, int32_t flags, const uint32_t
   if (!b || !sobol_m || sobol_dims <= 0) return QIW_ERR_ARG;
   if (precision != QIW_PREC_FP64 && precision != QIW_PREC_FP32) return b->fail(QIW_ERR_ARG, "qiw_batch_run: precision");
   if (b->solves.empty()) return QIW_OK;
-  cudaSetDevice(b->device);
+  qiw::DeviceScope dev_scope(b->device);
+  if (dev_scope.status != cudaSuccess) return b->fail(QIW_ERR_CUDA, std::string("qiw_batch_run: cudaSetDevice: ") + cudaGetErrorString(dev_scope.status));
   int rc;
   for (const PlanEntry &e : b->plans)
     if (e.rec->plan.D > sobol_dims) return b->fail(QIW_ERR_ARG, "qiw_batch_run: Sobol table has too few dimensions");
@@ -547,13 +549,16 @@ int qiw_batch_run(qiw_batch *b, int32_t precision, int32_t flags, const uint32_t
   b->st.n_plans = (int)b->plans.size();
   b->st.n_tiles_bold = (int64_t)P.bold.tiles.size();
   b->st.n_tiles_bare = (int64_t)P.bare.tiles.size();
+  if (errw & 2)
+    return b->fail(QIW_ERR_DEVICE, "qiw_batch_run: normalize!: the largest diagonal of P is not positive (no log)");
   if (errw) return b->fail(QIW_ERR_DEVICE, "qiw_batch_run: non-finite result");
   return QIW_OK;
 }
 
 int qiw_batch_get_P(qiw_batch *b, int32_t id, double *P) {
   if (!b || !P || id < 0 || id >= (int)b->solves.size()) return QIW_ERR_ARG;
-  cudaSetDevice(b->device);
+  qiw::DeviceScope dev_scope(b->device);
+  if (dev_scope.status != cudaSuccess) return b->fail(QIW_ERR_CUDA, std::string("qiw_batch_get_P: cudaSetDevice: ") + cudaGetErrorString(dev_scope.status));
   SolveRec *s = b->solves[id];
   std::vector<double> t(s->ctx->ptab_size);
   int rc;

@@ -85,10 +85,12 @@ __global__ void batch_finish_kernel(const BatchSolve *__restrict__ solves, const
 // One CTA per solve: i*P(tau_j), j = step + 1, is the sum of the step's work items -- per
 // order first, then over orders, as the host does -- (src/ppgf.jl:474-504); after a bold
 // step every tau is rescaled by exp(-tau lambda), lambda = log(max_s,i i*P_s,ii(tau_j)) / tau_j
-// (normalize!(P, tau), src/ppgf.jl:646-654).  The FP32 copy is refreshed.
+// (normalize!(P, tau), src/ppgf.jl:646-654).  The FP32 copy is refreshed.  A largest diagonal
+// that is not positive and finite has no logarithm: the solve's P is left unscaled and bit 1
+// of the error word is set (the host reports QIW_ERR_DEVICE, as normalize_tau raises on it).
 __global__ void batch_update_kernel(const DevProblem *__restrict__ probs, const BatchSolve *__restrict__ solves,
                                     const BatchWork *__restrict__ works, const double *__restrict__ res,
-                                    int step) {
+                                    int *err_word, int step) {
   const BatchSolve &so = solves[blockIdx.x];
   if (step > so.last_step) return;
   const DevProblem &pb = probs[blockIdx.x];
@@ -123,7 +125,9 @@ __global__ void batch_update_kernel(const DevProblem *__restrict__ probs, const 
         const int d = pb.dims[s];
         for (int i = 0; i < d; ++i) pmax = fmax(pmax, nv[pb.res_off[s] + i * d + i]);
       }
-      const double lam = log(pmax) / so.taus[j];
+      double lam = 0.0;
+      if (pmax > 0.0 && isfinite(pmax)) lam = log(pmax) / so.taus[j];
+      else atomicOr(err_word, 2);
       s_lam = lam;
       so.lam[j] = lam;
     }
@@ -205,7 +209,7 @@ cudaError_t launch_batch_reset(const BatchArgs &a) {
 }
 
 cudaError_t launch_batch_update(const BatchArgs &a) {
-  batch_update_kernel<<<a.n_solves, 128, 0, a.stream>>>(a.probs, a.solves, a.works, a.res, a.step);
+  batch_update_kernel<<<a.n_solves, 128, 0, a.stream>>>(a.probs, a.solves, a.works, a.res, a.err_word, a.step);
   return cudaGetLastError();
 }
 

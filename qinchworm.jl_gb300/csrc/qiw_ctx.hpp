@@ -39,6 +39,24 @@ struct DevBuf {
   }
 };
 
+// Makes a context's device current for one library call and gives the caller's thread its
+// previous current device back when the call returns, so no entry point leaves another device
+// current behind.  `status` is the result of the switch; a call that needs the device checks it.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t status = cudaSuccess;
+  explicit DeviceScope(int device) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != device) status = cudaSetDevice(device);
+    if (status != cudaSuccess || prev == device) prev = -1;   // nothing to give back
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope &) = delete;
+  DeviceScope &operator=(const DeviceScope &) = delete;
+};
+
 struct GroupRec {
   Plan plan;
   DevBuf<PmJob> pm;

@@ -36,11 +36,17 @@ constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 void *g_scratch_addr[kMaxDevices] = {nullptr};
 
-// Device address of g_qiw_noalloc_scratch on the current device (looked up once).
+// Device address of g_qiw_noalloc_scratch on `device`, which must be the current device
+// (looked up once per device and cached; a lookup made with another device current would
+// cache that device's copy, so it is refused).
 cudaError_t scratch_address(int device, unsigned char **out) {
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_scratch_mutex);
   if (!g_scratch_addr[device]) {
+    int cur = -1;
+    cudaError_t e0 = cudaGetDevice(&cur);
+    if (e0 != cudaSuccess) return e0;
+    if (cur != device) return cudaErrorInvalidDevice;
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_qiw_noalloc_scratch);
     if (e != cudaSuccess) return e;
@@ -58,7 +64,8 @@ extern "C" int qiw_integrate_noalloc(qiw_ctx *c, int32_t n_work, const qiw_work_
                                      double *out_device) {
   using namespace qiw;
   if (!c || n_work < 0 || (n_work > 0 && (!work || !out_device))) return QIW_ERR_ARG;
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_integrate_noalloc: cudaSetDevice");
   if (n_work == 0) return QIW_OK;
   LaunchTables t;
   int rc = prepare_launch(c, n_work, work, precision, &t);

@@ -348,7 +348,8 @@ extern "C" {
 int qiw_warp_create(qiw_ctx *c, int32_t D, uint64_t seed, int32_t *warp_id) {
   if (!c || !warp_id) return QIW_ERR_ARG;
   if (D < 2 || D > WDMAX) return c->fail(QIW_ERR_UNSUPPORTED, "qiw_warp_create: dimension must lie in 2..8");
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_warp_create: cudaSetDevice");
   Layout L(D);
   WarpRec *w = new WarpRec();
   w->D = D;
@@ -409,6 +410,8 @@ int qiw_warp_n_params(qiw_ctx *c, int32_t id, int64_t *n) {
 
 int qiw_warp_get_params(qiw_ctx *c, int32_t id, double *out) {
   if (!c || !out || id < 0 || id >= (int)c->warps.size()) return QIW_ERR_ARG;
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_warp_get_params: cudaSetDevice");
   WarpRec *w = c->warps[id];
   const int n = Layout(w->D).n;
   std::vector<float> p(n);
@@ -420,6 +423,8 @@ int qiw_warp_get_params(qiw_ctx *c, int32_t id, double *out) {
 
 int qiw_warp_set_params(qiw_ctx *c, int32_t id, const double *in) {
   if (!c || !in || id < 0 || id >= (int)c->warps.size()) return QIW_ERR_ARG;
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_warp_set_params: cudaSetDevice");
   WarpRec *w = c->warps[id];
   const int n = Layout(w->D).n;
   std::vector<float> p(n);
@@ -466,7 +471,8 @@ static int run_grad(qiw_ctx *c, WarpRec *w, const float *X, const float *wt, int
 int qiw_warp_grad(qiw_ctx *c, int32_t id, const double *x, const double *wt, int64_t n, double *grad_out,
                   double *loss_out) {
   if (!c || !x || !wt || !grad_out || id < 0 || id >= (int)c->warps.size() || n <= 0) return QIW_ERR_ARG;
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_warp_grad: cudaSetDevice");
   WarpRec *w = c->warps[id];
   int rc = upload_batch(c, w, x, wt, n);
   if (rc || (rc = run_grad(c, w, w->X.p, w->w.p, n))) return rc;
@@ -486,7 +492,8 @@ int qiw_warp_train(qiw_ctx *c, int32_t id, const double *x, const double *wt, in
                    int32_t batch, double lr, double *final_loss) {
   if (!c || !x || !wt || id < 0 || id >= (int)c->warps.size() || n <= 0 || steps < 0 || batch <= 0)
     return QIW_ERR_ARG;
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_warp_fit: cudaSetDevice");
   WarpRec *w = c->warps[id];
   // whole-set normalisation; minibatch b covers samples [b*batch, (b+1)*batch) cyclically
   int rc = upload_batch(c, w, x, wt, n);
@@ -520,7 +527,8 @@ int qiw_warp_train(qiw_ctx *c, int32_t id, const double *x, const double *wt, in
 int qiw_warp_map(qiw_ctx *c, int32_t id, const uint32_t *m, const uint32_t *x0, uint64_t first, uint64_t n,
                  double *pts_out) {
   if (!c || !m || !x0 || !pts_out || id < 0 || id >= (int)c->warps.size()) return QIW_ERR_ARG;
-  cudaSetDevice(c->device);
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_warp_map: cudaSetDevice");
   WarpRec *w = c->warps[id];
   DevBuf<uint32_t> dm;
   DevBuf<double> dp;

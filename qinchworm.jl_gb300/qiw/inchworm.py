@@ -110,9 +110,11 @@ def _randomized(groups, sobol, launch, stat):
     with the reference's draws: groups in order, group g draws the scramble of sequence s only
     when it evaluates it, and stops after s > 1 once the largest |std(samples[1:s])| is at most
     target_std.  Unscrambled sequences are all the same sequence: one evaluation, std 0 (NaN for
-    N_seqs = 1, as Julia's std of one sample).
+    N_seqs = 1, as Julia's std of one sample).  D = 0 marks an exact group (order 0, and order 1
+    of the self-energy, src/inchworm.jl:566-571): one evaluation, no draws, std 0.
 
-    groups[i] is None or (D, RandomizationParams); launch(items), items a list of (i, [(m, x0),
+    groups[i] is None or (D, RandomizationParams), D the dimension of the scrambled sequence
+    (2k; the kernel may read fewer coordinates); launch(items), items a list of (i, [(m, x0),
     ...]) (m None for D = 0), returns {i: [all-reduced packed value per sequence]} from one
     qiw_integrate call; stat(i, v) is the quantity the statistics apply to.  Every sequence of
     every pending group runs in one launch; when a group stops early, the scrambling generators
@@ -139,8 +141,8 @@ def _randomized(groups, sobol, launch, stat):
             D, rp = groups[i]
             vs = np.array([stat(i, v) for v in vals[i]])
             if D == 0 or rp.rng is None:
-                n = 1 if D == 0 else rp.N_seqs
-                out[i] = (vs[0], np.full(vs.shape[1], np.nan) if n == 1 else np.zeros(vs.shape[1]))
+                exact_or_many = D == 0 or rp.N_seqs > 1
+                out[i] = (vs[0], np.zeros(vs.shape[1]) if exact_or_many else np.full(vs.shape[1], np.nan))
                 continue
             k = len(vs)
             for s_ in range(2, len(vs) + 1):
@@ -204,6 +206,10 @@ class _Session:
                 entries.append(None)
                 continue
             entries.append((self.group(kind, td, corr), td, D))
+        # Scrambled-sequence dimension: 2k for every sampled group.  Self-energy groups integrate
+        # 2k - 2 times but the reference draws a 2k-dimensional sequence and the transform reads
+        # its first 2k - 2 coordinates (src/inchworm.jl:582-594), so the kernel gets those rows.
+        seq_dims = [None if e is None else (0 if e[2] == 0 else 2 * e[1].order) for e in entries]
 
         def launch(items):
             # one launch for every (group, sequence) of the step
@@ -212,6 +218,8 @@ class _Session:
                 gid, td, D = entries[i]
                 start, length = (0, 1) if D == 0 else rank_sub_range(td.N_samples, comm)  # exact: once per rank
                 for m, x0 in seqs:
+                    if m is not None and m.shape[0] > D:
+                        m, x0 = np.ascontiguousarray(m[:D]), np.ascontiguousarray(x0[:D])
                     works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
                     index.append(i)
             wl = [warps.get(w.group, -1) for w in works] if warps else None
@@ -236,7 +244,7 @@ class _Session:
             return vals
 
         # per group (mean, std) as packed vectors in sector order (see _pack_blocks)
-        return _randomized([None if e is None else (e[2], e[1].rand_params) for e in entries],
+        return _randomized([None if e is None else (sd, e[1].rand_params) for e, sd in zip(entries, seq_dims)],
                            self.dev.sobol, launch, lambda i, v: v)
 
 

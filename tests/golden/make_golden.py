@@ -8,7 +8,7 @@ Reads (never executes) the reference repository:
   * README.md                  Z and rho of the README Anderson run (README.md:203-204)
 and writes small JSON files that the tests use on machines without the reference.
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_golden.py /path/to/QInchworm.jl   (or QINCHWORM_REF=/path/to/QInchworm.jl)
 """
 from __future__ import annotations
 
@@ -104,7 +104,9 @@ def readme_output(ref: str):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QINCHWORM_REF")
+    if not ref:
+        sys.exit("usage: make_golden.py <path to a QInchworm.jl checkout> (or set QINCHWORM_REF)")
     inchworm_h5(ref)
     topology_eval_h5(ref)
     sobol_vectors(ref)

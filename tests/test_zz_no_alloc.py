@@ -19,7 +19,7 @@ from qiw.diagrammatics import get_topologies_at_order
 
 pytestmark = pytest.mark.gpu
 
-REL64 = 1e-12
+REL = {_lib.QIW_PREC_FP64: 1e-12, _lib.QIW_PREC_FP32: 1e-4}
 
 
 def _descs(device, works):
@@ -35,7 +35,8 @@ def _descs(device, works):
     return descs, keep
 
 
-def test_noalloc_matches_integrate_twice(device):
+@pytest.mark.parametrize("precision", [_lib.QIW_PREC_FP64, _lib.QIW_PREC_FP32])
+def test_noalloc_matches_integrate_twice(device, precision):
     import torch
     exp = models.eg_discrete_bath(n_tau=48)
     g = exp.grid
@@ -48,11 +49,11 @@ def test_noalloc_matches_integrate_twice(device):
     lib = device.lib
     for call, (n, N) in enumerate([(17, 384), (21, 256)]):
         works = [Work(gid, g.tau(0), g.tau(n), g.tau(n + 1), 0, N, N) for gid in gids]
-        want = device.integrate(works)
+        want = device.integrate(works, precision)
         descs, keep = _descs(device, works)
         out = torch.full((2 * rs * len(works),), float("nan"), dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
-        rc = lib.qiw_integrate_noalloc(device.h, len(works), descs, _lib.QIW_PREC_FP64, C.c_void_p(out.data_ptr()))
+        rc = lib.qiw_integrate_noalloc(device.h, len(works), descs, precision, C.c_void_p(out.data_ptr()))
         assert rc == _lib.QIW_OK, lib.qiw_last_error(device.h).decode()
         z = out.cpu().numpy()
         z = z[0::2] + 1j * z[1::2]
@@ -60,7 +61,7 @@ def test_noalloc_matches_integrate_twice(device):
             ref = np.concatenate([b.ravel(order="F") for b in blocks])
             got = z[i * rs:(i + 1) * rs]
             scale = np.abs(ref).max()
-            assert np.abs(got - ref).max() <= REL64 * scale, (call, i)
+            assert np.abs(got - ref).max() <= REL[precision] * scale, (call, i)
 
 
 def test_noalloc_rejects_oversized_calls(device):
@@ -70,10 +71,14 @@ def test_noalloc_rejects_oversized_calls(device):
     device.set_ppgf(exp.P)
     gid = device.create_group(_lib.QIW_GROUP_BOLD, 1, 1, get_topologies_at_order(1, 1))
     g = exp.grid
-    # 2^25 samples: 524288 CTAs whose map and partial sums need more than 16 MiB
-    works = [Work(gid, g.tau(0), g.tau(3), g.tau(4), 0, 1 << 25, 1 << 25)]
+    # 2^27 samples: at most 128 samples per tile (any thread setting), at least 2^20 CTAs whose
+    # map and partial sums need far more than the 16 MiB array
+    works = [Work(gid, g.tau(0), g.tau(3), g.tau(4), 0, 1 << 27, 1 << 27)]
     descs, keep = _descs(device, works)
     out = torch.zeros(8, dtype=torch.float64, device="cuda")
     rc = device.lib.qiw_integrate_noalloc(device.h, 1, descs, _lib.QIW_PREC_FP64, C.c_void_p(out.data_ptr()))
     assert rc == _lib.QIW_ERR_MEMORY
-    assert b"maximum" in device.lib.qiw_last_error(device.h)
+    msg = device.lib.qiw_last_error(device.h).decode()
+    assert "maximum" in msg
+    needed = int(msg.split("needs ")[1].split(" bytes")[0])
+    assert needed > 16 << 20
