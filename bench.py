@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--model", default="eg", choices=["eg", "anderson", "t2g", "anderson_b40"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the GPU-vs-oracle check of the benchmarked step")
     ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy", "batch", "warp", "correlators"])
     ap.add_argument("--step", type=int, default=200, help="warp mode: inch step (tau_w index) the warps are fitted at")
     ap.add_argument("--warp-groups-only", action="store_true",
@@ -144,14 +145,13 @@ def fp64_peak_tflops() -> float:
     return 2.0 * 4096 ** 3 / best / 1e12
 
 
-def cpu_baseline(exp, tds, samples_cap: int, budget_s: float = 15.0):
-    """Oracle (C restatement of the reference evaluator) on one inch step, all host cores,
-    bounded number of samples per group; returns (topology-samples/s, cores, description)."""
+def cpu_baseline(exp, tds, samples_cap: int, n: int, budget_s: float = 15.0):
+    """Oracle (C restatement of the reference evaluator) on inch step n (tau_w index n), all host
+    cores, bounded number of samples per group; returns (topology-samples/s, cores, description)."""
     import oracle as orc
     cores = os.cpu_count() or 1
     pb = orc.OracleProblem(exp)
     g = exp.grid
-    n = g.n_tau // 2
     t = (g.tau(0), g.tau(n), g.tau(n + 1))
     # calibrate on the heaviest group
     heavy = max(tds, key=lambda td: (td.order, len(td.topologies)))
@@ -175,6 +175,66 @@ def cpu_baseline(exp, tds, samples_cap: int, budget_s: float = 15.0):
     return units / el, cores, f"one inch step (tau_w index {n}), {N} Sobol samples per group, {len(tds)} groups"
 
 
+def parity_check(dev, ses, exp, tds, t, prec, slices):
+    """GPU vs oracle on the benchmarked step's groups after the timed region: every sampled group
+    on Sobol slices [first, first + n) of its N-point sequence (weights of the full sequence, as
+    one rank of rank_sub_range), the exact order 0 once; the oracle runs on all host cores.
+    Returns the parity record of the bench line."""
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle as orc
+    from qiw import _lib
+    from qiw.device import Work
+    dev.set_ppgf(exp.P)
+    ob = orc.OracleProblem(exp)
+    works, jobs = [], []
+    for td in tds:
+        gid = ses.group(_lib.QIW_GROUP_BOLD, td)
+        tl = [(x.pairs, x.parity) for x in td.topologies]
+        for (k, n) in ([(0, 1)] if td.order == 0 else slices):
+            N = 1 if td.order == 0 else td.N_samples
+            works.append(Work(gid, *t, k, n, N))
+            jobs.append((td.order, td.n_pts_after, tl, (k, n), N))
+    got = dev.integrate(works, prec)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        want = list(ex.map(lambda j: ob.integrate("bold", j[0], j[1], j[2], *t, j[4], sample_range=j[3]), jobs))
+    worst = 0.0
+    for a, w in zip(got, want):
+        scale = max(float(np.abs(x).max()) for x in w)
+        err = max(float(np.abs(x - y).max()) for x, y in zip(a, w))
+        worst = max(worst, err / scale if scale > 0 else err)
+    n_samp = sum(j[3][1] for j in jobs)
+    return {"max_rel_err": worst, "tol": 1e-12 if prec == 0 else 1e-4, "samples_checked": n_samp,
+            "topology_samples_checked": sum(j[3][1] * len(j[2]) for j in jobs), "work_items": len(jobs),
+            "slices": [list(x) for x in slices], "against": "CPU oracle (C restatement of src/topology_eval.jl)",
+            "oracle_s": time.perf_counter() - t0}
+
+
+def julia_probe():
+    """Whether the reference itself (pure Julia) could run on this host."""
+    import shutil
+    jl = shutil.which("julia")
+    if not jl:
+        return {"julia": None, "qinchworm_loads": False,
+                "note": "no julia on this host: the reference (pure Julia) cannot run here; the arm is the oracle port"}
+    out = {"julia": None, "qinchworm_loads": False}
+    try:
+        out["julia"] = subprocess.run([jl, "--version"], capture_output=True, text=True, timeout=60).stdout.strip()
+        r = subprocess.run([jl, "-e", "using QInchworm"], capture_output=True, text=True, timeout=300)
+        out["qinchworm_loads"] = r.returncode == 0
+        if r.returncode:
+            out["note"] = "QInchworm.jl or its dependencies are not installed: the arm is the oracle port"
+    except (OSError, subprocess.TimeoutExpired) as e:
+        out["note"] = f"julia probe failed: {e}"
+    return out
+
+
+def bench_config(desc, kmax, N, tds):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": desc + f", orders 0:{kmax}, one regular inch step per bench step",
+            "N_samples": N, "groups_per_step": len(tds), "topologies_per_step": sum(len(td.topologies) for td in tds)}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -182,19 +242,19 @@ def run_reference(args):
     exp, desc, kmax = workload(args.model)
     tds = bold_groups(range(0, kmax + 1), args.samples)
     vals = []
-    for i in range(args.warmup + args.steps):
-        v, cores, sample = cpu_baseline(exp, tds, args.samples, budget_s=8.0)
+    for i in range(args.warmup + args.steps):   # step i at tau_w index 1 + i, as the GPU arm steps
+        v, cores, sample = cpu_baseline(exp, tds, args.samples, 1 + i, budget_s=8.0)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": desc + f", orders 0:{kmax}, one regular inch step per bench step",
-                       "N_samples": args.samples, "groups_per_step": len(tds),
-                       "topologies_per_step": sum(len(td.topologies) for td in tds)},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": bench_config(desc, kmax, args.samples, tds),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample + f"; steps at tau_w indices {1 + args.warmup}..{args.warmup + args.steps}"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_probe": julia_probe()}
     print(json.dumps(line))
 
 
@@ -297,9 +357,8 @@ def run_ours(args):
         "value": units / k_tot, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * k_tot / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64acc", "data": "synthetic",
-        "config": {"workload": desc + f", orders 0:{kmax}, one regular inch step per bench step",
-                   "N_samples": N * world, "groups_per_step": len(tds),
-                   "topologies_per_step": sum(len(td.topologies) for td in tds), "l2": "256 MB write between timed steps"},
+        "config": bench_config(desc, kmax, N * world, tds),
+        "l2_flush": "256 MB write between timed steps",
         "e2e": {"value": units / w_tot, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * w_tot / args.steps},
         "roofline": {"bound": "fp64_pipe" if args.precision == "fp64" else "fp32_pipe", "achieved": achieved,
@@ -311,8 +370,13 @@ def run_ours(args):
         "gpu_launches": 2 * args.steps,
         "clocks": clocks,
     }
+    if not args.no_parity and world == 1:   # the benchmarked step against the oracle, after timing
+        N_all = N * world
+        starts = sorted({k for k in (0, N_all // 4 + 5, N_all // 2 + 11, max(N_all - 64, 0)) if k < N_all})
+        sl = [(k, min(64, N_all - k)) for k in starts]
+        line["parity"] = parity_check(dev, ses, exp, tds, (grid.tau(0), grid.tau(n), grid.tau(n + 1)), prec, sl)
     if not args.no_cpu_baseline and world == 1:   # the CPU leg runs at N = 1 only
-        v, cores, sample = cpu_baseline(exp, tds, N)
+        v, cores, sample = cpu_baseline(exp, tds, N, 1 + args.warmup + args.steps // 2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     print(json.dumps(line))
 

@@ -202,6 +202,15 @@ int qiw_integrate_samples(qiw_ctx *ctx, const qiw_work_desc *work, int32_t preci
 /* Kernel time of the most recent qiw_integrate (ms, CUDA events on the context stream). */
 double qiw_last_kernel_ms(const qiw_ctx *ctx);
 
+/* The kernels' own Sobol integers (test and debugging interface): points first .. first + n - 1
+ * of the D-dimensional sequence with direction numbers m [D][32] and digital shift x0 [D]
+ * (unscrambled: x0 = 0), computed on the device by the Gray-code jump the evaluation kernels
+ * use, written to out [n][D] (host buffer).  Point k is what the reference's next! returns on
+ * its (k+1)-th call, and skip!(seq, first, exact=true) starts the range at `first`
+ * (src/scrambled_sobol.jl:158-208).  first + n <= 2^32; n <= 2^26 per call. */
+int qiw_sobol_points(qiw_ctx *ctx, int32_t D, const uint32_t *m, const uint32_t *x0, uint64_t first,
+                     uint64_t n, uint32_t *out);
+
 /* No counterpart in the reference: measures this device's CUDA-core FMA throughput
  * (QIW_PREC_FP64: DFMA, QIW_PREC_FP32: FFMA) in TFLOP/s with independent FMA chains on
  * every SM, the roofline denominator of the evaluation kernels. */

@@ -79,6 +79,7 @@ def lib():
                                         C.c_int64, C.c_int, C.c_void_p]
         _lib.qiwo_sobol_directions.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         _lib.qiwo_sobol_points.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p]
+        _lib.qiwo_sobol_point_u32.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
         _lib.qiwo_natural_spline_M.argtypes = [C.c_int, C.c_double, C.c_void_p, C.c_void_p]
         _lib.qiwo_integrate_range.restype = C.c_int
         _lib.qiwo_integrate_range.argtypes = [C.POINTER(_Problem), C.POINTER(_Group), C.c_void_p, C.c_void_p,
@@ -109,6 +110,17 @@ def sobol_points(m: np.ndarray, x0: Optional[np.ndarray], skip: int, n: int) -> 
     x0 = np.zeros(D, np.uint32) if x0 is None else np.ascontiguousarray(x0, dtype=np.uint32)
     out = np.zeros((n, D))
     lib().qiwo_sobol_points(D, _ptr(m), _ptr(x0), skip, n, _ptr(out))
+    return out
+
+
+def sobol_point_u32(m: np.ndarray, x0: Optional[np.ndarray], n: int) -> np.ndarray:
+    """Point n (0-based) as UInt32 by the Gray-code closed form of next!'s recurrence."""
+    D = m.shape[0]
+    m = np.ascontiguousarray(m, dtype=np.uint32)
+    x0 = np.zeros(D, np.uint32) if x0 is None else np.ascontiguousarray(x0, dtype=np.uint32)
+    out = np.zeros(D, np.uint32)
+    if lib().qiwo_sobol_point_u32(D, _ptr(m), _ptr(x0), n, _ptr(out)):
+        raise ValueError("Sobol index beyond 2^32 - 1")
     return out
 
 

@@ -114,6 +114,23 @@ int qiwo_sobol_points(int D, const uint32_t *m, const uint32_t *x0, int64_t skip
     return 0;
 }
 
+/* Point n (0-based) as UInt32 by the closed form of next!'s recurrence: the shift XOR the
+ * columns m[:, b] over the set bits b of the Gray code n ^ (n >> 1).  Pinned against the
+ * sequential generator above (and SciPy's) in the tests; used where a sequential skip! to the
+ * index would take too long (n near 2^32). */
+int qiwo_sobol_point_u32(int D, const uint32_t *m, const uint32_t *x0, uint64_t n, uint32_t *out)
+{
+    if (n >> 32) return 1;
+    const uint64_t g = n ^ (n >> 1);
+    for (int d = 0; d < D; ++d) {
+        uint32_t v = x0 ? x0[d] : 0u;
+        for (int b = 0; b < 32; ++b)
+            if ((g >> b) & 1u) v ^= m[d * 32 + b];
+        out[d] = v;
+    }
+    return 0;
+}
+
 /* ------------------------------------------------------------------ transforms */
 
 static double simplex_volume(int d, double edge)

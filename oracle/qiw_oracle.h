@@ -68,6 +68,7 @@ typedef struct {
 
 int qiwo_sobol_directions(int D, const int64_t *poly, const int64_t *vinit, int vinit_cols, uint32_t *m);
 int qiwo_sobol_points(int D, const uint32_t *m, const uint32_t *x0, int64_t skip, int64_t n, double *out);
+int qiwo_sobol_point_u32(int D, const uint32_t *m, const uint32_t *x0, uint64_t n, uint32_t *out);
 void qiwo_natural_spline_M(int n, double h, const double *y, double *M);
 int qiwo_integrate(const qiwo_problem *pb, const qiwo_group *gr, const uint32_t *m, const uint32_t *x0,
                    int64_t N, int n_ranks, double *out);

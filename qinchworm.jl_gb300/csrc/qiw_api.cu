@@ -632,6 +632,35 @@ int qiw_integrate_samples(qiw_ctx *c, const qiw_work_desc *work, int32_t precisi
   return integrate_impl(c, 1, work, precision, out, nullptr, samples);
 }
 
+int qiw_sobol_points(qiw_ctx *c, int32_t D, const uint32_t *m, const uint32_t *x0, uint64_t first, uint64_t n,
+                     uint32_t *out) {
+  if (!c || !m || !x0 || (n > 0 && !out)) return QIW_ERR_ARG;
+  if (D < 1 || D > kMaxDim) return c->fail(QIW_ERR_ARG, "qiw_sobol_points: D must lie in 1..32");
+  if (first > (1ull << 32) || n > (1ull << 32) - first)
+    return c->fail(QIW_ERR_ARG, "qiw_sobol_points: points beyond index 2^32 - 1 (32 direction numbers)");
+  if (n > (1ull << 26)) return c->fail(QIW_ERR_ARG, "qiw_sobol_points: at most 2^26 points per call");
+  if (n == 0) return QIW_OK;
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_sobol_points: cudaSetDevice");
+  DevBuf<uint32_t> dm, dx, dout;
+  int rc;
+  if ((rc = c->cuda(dm.upload(m, (size_t)D * 32, c->stream), "qiw_sobol_points: upload")) ||
+      (rc = c->cuda(dx.upload(x0, (size_t)D, c->stream), "qiw_sobol_points: upload")) ||
+      (rc = c->cuda(dout.reserve((size_t)n * D), "qiw_sobol_points: alloc")) ||
+      (rc = c->cuda(launch_sobol_points(dm.p, dx.p, D, first, n, dout.p, c->stream), "qiw_sobol_points: launch")) ||
+      (rc = c->cuda(cudaMemcpyAsync(out, dout.p, sizeof(uint32_t) * n * D, cudaMemcpyDeviceToHost, c->stream),
+                    "qiw_sobol_points: download")) ||
+      (rc = c->cuda(cudaStreamSynchronize(c->stream), "qiw_sobol_points"))) {
+    cudaStreamSynchronize(c->stream);
+    dm.release(); dx.release(); dout.release();
+    return rc;
+  }
+  dm.release();
+  dx.release();
+  dout.release();
+  return QIW_OK;
+}
+
 int qiw_measure_fma_peak(qiw_ctx *c, int32_t precision, double *tflops) {
   if (!c || !tflops) return QIW_ERR_ARG;
   qiw::DeviceScope dev_scope(c->device);

@@ -68,6 +68,18 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// Coordinate of Sobol point n (0-based) by the Gray-code jump: x0 ^ XOR of md[b] over the set
+// bits b of gray = n ^ (n >> 1).  It is the value the reference's next! returns on its (n+1)-th
+// call (src/scrambled_sobol.jl:158-173: the first call returns the shift, call n+1 XORs column
+// ctz(n) into it), so skip!(seq, k, exact=true) becomes a start at n = k (src/scrambled_sobol.jl:189-208).
+__device__ __forceinline__ uint32_t sobol_coord(const uint32_t *__restrict__ md, uint32_t x0d, uint32_t gray) {
+  uint32_t v = x0d;
+#pragma unroll 8
+  for (int b = 0; b < 32; ++b)
+    if ((gray >> b) & 1u) v ^= __ldg(md + b);
+  return v;
+}
+
 // Linear interpolation of a uniform-grid table at dt >= 0 (rule of qiw/gf.py: linear_interp).
 __device__ __forceinline__ void lin_index(double dt, double inv_h, int n_tau, int *i, double *f) {
   double x = dt * inv_h;
@@ -438,14 +450,8 @@ __device__ __forceinline__ void sample_setup(const DevProblem &pb, const DevGrou
         wt = pp[D];
       } else {
 #pragma unroll 1
-        for (int d = 0; d < D; ++d) {
-          uint32_t v = __ldg(w.x0 + d);
-          const uint32_t *md = w.m + d * 32;
-#pragma unroll 8
-          for (int b = 0; b < 32; ++b)
-            if ((gray >> b) & 1u) v ^= __ldg(md + b);
-          u[d] = ldexp((double)v, -32);  // exact: ldexp(Float64(x), -32)
-        }
+        for (int d = 0; d < D; ++d)
+          u[d] = ldexp((double)sobol_coord(w.m + d * 32, __ldg(w.x0 + d), gray), -32);  // exact: ldexp(Float64(x), -32)
       }
       bool mapped = false;  // the alternative maps of bare groups live in the extras kernel
       if constexpr (EXTRAS) {

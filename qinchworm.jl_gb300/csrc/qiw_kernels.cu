@@ -53,6 +53,25 @@ cudaError_t launch_fma_peak(bool fp32, void *out, int blocks, int threads, int i
   return cudaGetLastError();
 }
 
+// The kernels' Sobol integers for points first .. first + n - 1 (the same sobol_coord the
+// evaluation kernels use), out[i][d] row-major.
+__global__ void sobol_points_kernel(const uint32_t *__restrict__ m, const uint32_t *__restrict__ x0, int D,
+                                    uint64_t first, uint64_t n, uint32_t *__restrict__ out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t k = first + i;
+  const uint32_t gray = (uint32_t)(k ^ (k >> 1));
+  for (int d = 0; d < D; ++d) out[i * D + d] = sobol_coord(m + d * 32, __ldg(x0 + d), gray);
+}
+
+cudaError_t launch_sobol_points(const uint32_t *m, const uint32_t *x0, int D, uint64_t first, uint64_t n,
+                                uint32_t *out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  sobol_points_kernel<<<blocks, 256, 0, st>>>(m, x0, D, first, n, out);
+  return cudaGetLastError();
+}
+
 template <typename T, int ARENA, int RESMAX>
 static cudaError_t launch_t(const LaunchArgs &a) {
   eval_kernel<T, ARENA, RESMAX, false><<<a.n_cta, a.threads, eval_smem_bytes(a.threads, RESMAX, a.stage), a.stream>>>(a.pb, a.groups, a.works, a.cta_map,

@@ -38,7 +38,7 @@ EXPORTS = ["qiw_ctx_create", "qiw_ctx_destroy", "qiw_last_error", "qiw_problem_s
            "qiw_warp_get_params", "qiw_warp_set_params", "qiw_warp_grad", "qiw_warp_train", "qiw_warp_map",
            "qiw_integrate_warped", "qiw_integrate_samples", "qiw_batch_create", "qiw_batch_destroy",
            "qiw_batch_last_error", "qiw_batch_add", "qiw_batch_run", "qiw_batch_get_P", "qiw_batch_stats_get",
-           "qiw_plan_cache_info", "qiw_plan_cache_clear"]
+           "qiw_plan_cache_info", "qiw_plan_cache_clear", "qiw_sobol_points"]
 
 QIW_BATCH_GRAPH = 1
 QIW_BATCH_AUTOTUNE = 2
@@ -110,6 +110,8 @@ def load(path: Optional[str] = None) -> C.CDLL:
     lib.qiw_last_kernel_ms.argtypes = [C.c_void_p]
     lib.qiw_last_kernel_ms.restype = C.c_double
     lib.qiw_measure_fma_peak.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
+    lib.qiw_sobol_points.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64,
+                                     C.c_void_p]
     lib.qiw_integrate_noalloc.argtypes = [C.c_void_p, C.c_int32, C.POINTER(WorkDesc), C.c_int32, C.c_void_p]
     lib.qiw_warp_create.argtypes = [C.c_void_p, C.c_int32, C.c_uint64, C.POINTER(C.c_int32)]
     lib.qiw_warp_set_mix.argtypes = [C.c_void_p, C.c_int32, C.c_double]

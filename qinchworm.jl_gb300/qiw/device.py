@@ -202,6 +202,16 @@ class Device:
         self._check(self.lib.qiw_warp_map(self.h, wid, m.ctypes.data, x0.ctypes.data, first, n, pts.ctypes.data))
         return pts
 
+    def sobol_points(self, m: np.ndarray, x0: Optional[np.ndarray], first: int, n: int) -> np.ndarray:
+        """The kernels' Sobol integers (qiw_sobol_points): uint32 array [n][D] of points
+        first .. first + n - 1 for direction numbers m [D][32] and shift x0 [D]."""
+        m = np.ascontiguousarray(m, dtype=np.uint32)
+        D = m.shape[0]
+        x0 = np.ascontiguousarray(np.zeros(D, np.uint32) if x0 is None else x0, dtype=np.uint32)
+        out = np.zeros((n, D), np.uint32)
+        self._check(self.lib.qiw_sobol_points(self.h, D, m.ctypes.data, x0.ctypes.data, first, n, out.ctypes.data))
+        return out
+
     def fma_peak_tflops(self, precision: int = _lib.QIW_PREC_FP64) -> float:
         v = C.c_double()
         self._check(self.lib.qiw_measure_fma_peak(self.h, precision, C.byref(v)))
