@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--model", default="eg", choices=["eg", "anderson", "t2g", "anderson_b40"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the GPU-vs-oracle check of the benchmarked step")
+    ap.add_argument("--no-time-to-tol", action="store_true",
+                    help="skip the time-to-tolerance comparison (warped FP32 vs plain FP64) on the eg model")
     ap.add_argument("--mode", default="throughput", choices=["throughput", "accuracy", "batch", "warp", "correlators"])
     ap.add_argument("--step", type=int, default=200, help="warp mode: inch step (tau_w index) the warps are fitted at")
     ap.add_argument("--warp-groups-only", action="store_true",
@@ -208,6 +210,83 @@ def parity_check(dev, ses, exp, tds, t, prec, slices):
             "topology_samples_checked": sum(j[3][1] * len(j[2]) for j in jobs), "work_items": len(jobs),
             "slices": [list(x) for x in slices], "against": "CPU oracle (C restatement of src/topology_eval.jl)",
             "oracle_s": time.perf_counter() - t0}
+
+
+def time_to_tol(dev, step=200, n_loop=256, tols=(1e-3, 1e-4), n_ref=2 ** 20, n_max=2 ** 16):
+    """Time to a target error on one late eg inch step: warped FP32 (learned warps fitted on the
+    step's groups, fit time included) against plain FP64, errors max|sum of the step's groups -
+    reference| / max|reference|, reference = plain FP64 at n_ref samples per group.  P comes from
+    a plain GPU inchworm loop up to the step (n_loop samples).  A tolerance counts as resolved
+    only where the reference's own error (plain vs warped estimate at n_ref) is below half of it."""
+    import torch
+    from qiw import _lib, models
+    from qiw import warp as qwarp
+    from qiw.device import Work
+    from qiw.diagrammatics import get_topologies_at_order
+    from qiw.inchworm import inchworm
+    exp = models.eg_discrete_bath(n_tau=256)
+    g = exp.grid
+    t0 = time.perf_counter()
+    inchworm(exp, range(0, 5), range(0, 5), n_loop, dev=dev, n_steps=step - 1)
+    loop_s = time.perf_counter() - t0
+    dev.set_ppgf(exp.P)
+    t = (g.tau(0), g.tau(step), g.tau(step + 1))
+    gids = []
+    for o in range(0, 5):
+        for npa in ([0] if o == 0 else range(1, 2 * o)):
+            tops = get_topologies_at_order(o, npa)
+            if tops:
+                gids.append((o, dev.create_group(_lib.QIW_GROUP_BOLD, o, npa, tops)))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    wmap, kept = {}, 0
+    for (o, gid) in gids:
+        if o == 0:
+            continue
+        fit = qwarp.fit_group_warp(dev, Work(gid, *t, 0, 0, 0))
+        wmap[gid] = -1 if fit.warp_id is None else fit.warp_id
+        kept += fit.warp_id is not None
+    torch.cuda.synchronize()
+    fit_s = time.perf_counter() - t0
+
+    def total(N, prec, warped):
+        works = [Work(gid, *t, 0, N, N) for (_, gid) in gids]
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        res = dev.integrate(works, prec, warps=[wmap.get(gid, -1) for (_, gid) in gids] if warped else None)
+        el = time.perf_counter() - a
+        return np.concatenate([sum(r[s_] for r in res).ravel() for s_ in range(len(res[0]))]), el
+
+    ref, ref_s = total(n_ref, _lib.QIW_PREC_FP64, False)
+    ref_w, _ = total(n_ref, _lib.QIW_PREC_FP32, True)
+    sc = float(np.abs(ref).max())
+    ref_err = float(np.abs(ref - ref_w).max()) / sc
+    sweep, N = [], 2 ** 8
+    while N <= n_max:
+        vp, sp = total(N, _lib.QIW_PREC_FP64, False)
+        vw, sw = total(N, _lib.QIW_PREC_FP32, True)
+        sweep.append({"N": N, "err_plain_fp64": float(np.abs(vp - ref).max()) / sc, "s_plain_fp64": sp,
+                      "err_warped_fp32": float(np.abs(vw - ref).max()) / sc, "s_warped_fp32": sw})
+        N *= 2
+    out = {"workload": "eg Kanamori U=2 J=0.2 beta=8 n_tau=256, orders 0:4, inch step tau_w index %d" % step,
+           "reference": f"plain FP64, {n_ref} samples per group ({ref_s:.1f} s)", "reference_err": ref_err,
+           "fit_s": fit_s, "warps_kept": kept, "groups": len(gids) - 1, "loop_to_step_s": loop_s, "sweep": sweep,
+           "target_speedup": 10.0}
+    for tol in tols:
+        key = f"{tol:g}"
+        if ref_err > 0.5 * tol:
+            out[key] = {"resolved": False, "why": f"the reference's own error {ref_err:.1e} is above tol/2"}
+            continue
+        p = next((r for r in sweep if r["err_plain_fp64"] <= tol), None)
+        w = next((r for r in sweep if r["err_warped_fp32"] <= tol), None)
+        rec = {"resolved": True, "plain_fp64_N": p and p["N"], "plain_fp64_s": p and p["s_plain_fp64"],
+               "warped_fp32_N": w and w["N"], "warped_fp32_s": w and w["s_warped_fp32"]}
+        if p and w:
+            rec["speedup_fit_included"] = p["s_plain_fp64"] / (w["s_warped_fp32"] + fit_s)
+            rec["speedup_step_only"] = p["s_plain_fp64"] / w["s_warped_fp32"]
+            rec["speedup_fit_amortised_over_50_steps"] = p["s_plain_fp64"] / (w["s_warped_fp32"] + fit_s / 50)
+        out[key] = rec
+    return out
 
 
 def julia_probe():
@@ -375,6 +454,8 @@ def run_ours(args):
         starts = sorted({k for k in (0, N_all // 4 + 5, N_all // 2 + 11, max(N_all - 64, 0)) if k < N_all})
         sl = [(k, min(64, N_all - k)) for k in starts]
         line["parity"] = parity_check(dev, ses, exp, tds, (grid.tau(0), grid.tau(n), grid.tau(n + 1)), prec, sl)
+    if not args.no_time_to_tol and world == 1 and args.model == "eg":
+        line["time_to_tol"] = time_to_tol(dev)
     if not args.no_cpu_baseline and world == 1:   # the CPU leg runs at N = 1 only
         v, cores, sample = cpu_baseline(exp, tds, N, 1 + args.warmup + args.steps // 2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}

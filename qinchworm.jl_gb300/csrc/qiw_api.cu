@@ -253,6 +253,8 @@ int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const De
   la.partials = partials;
   la.n_cta = n_cta;
   la.threads = c->threads;
+  la.extra_smem = c->eval_extra_smem;
+  la.carveout = c->eval_carveout;
   la.arena_max = t.arena_max;
   la.res_max = t.res_max;
   la.fp32 = precision == QIW_PREC_FP32;
@@ -430,6 +432,8 @@ int qiw_ctx_create(qiw_ctx **out, int device) {
     int v = std::atoi(t);
     if (v == 32 || v == 64 || v == 96 || v == 128) c->threads = v;
   }
+  if (const char *t = std::getenv("QIW_EVAL_EXTRA_SMEM")) c->eval_extra_smem = std::max(0, std::min(160 << 10, std::atoi(t)));
+  if (const char *t = std::getenv("QIW_EVAL_CARVEOUT")) c->eval_carveout = std::max(-1, std::min(100, std::atoi(t)));
   *out = c;
   return QIW_OK;
 }

@@ -114,6 +114,8 @@ struct qiw_ctx {
   qiw::DevBuf<double> d_pts, d_samples;
   std::vector<qiw::WarpRec *> warps;
   int threads = 64;
+  int eval_extra_smem = 0;     // tuning: extra dynamic shared memory per CTA (limits CTAs per SM)
+  int eval_carveout = -1;      // tuning: preferred shared-memory carveout in percent (-1: driver default)
 
   int fail(int code, const std::string &msg) {
     err = msg;

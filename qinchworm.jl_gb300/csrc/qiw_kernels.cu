@@ -74,8 +74,14 @@ cudaError_t launch_sobol_points(const uint32_t *m, const uint32_t *x0, int D, ui
 
 template <typename T, int ARENA, int RESMAX>
 static cudaError_t launch_t(const LaunchArgs &a) {
-  eval_kernel<T, ARENA, RESMAX, false><<<a.n_cta, a.threads, eval_smem_bytes(a.threads, RESMAX, a.stage), a.stream>>>(a.pb, a.groups, a.works, a.cta_map,
-                                                                              a.partials);
+  const size_t smem = eval_smem_bytes(a.threads, RESMAX, a.stage) + (size_t)a.extra_smem;
+  auto *k = eval_kernel<T, ARENA, RESMAX, false>;
+  cudaError_t e;
+  if (smem > (48u << 10) && (e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+    return e;
+  if (a.carveout >= 0 && (e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, a.carveout)))
+    return e;
+  k<<<a.n_cta, a.threads, smem, a.stream>>>(a.pb, a.groups, a.works, a.cta_map, a.partials);
   return cudaGetLastError();
 }
 

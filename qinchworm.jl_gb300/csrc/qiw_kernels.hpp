@@ -31,6 +31,8 @@ struct LaunchArgs {
   bool fp32;
   bool extras;               // a work item has warped points or per-sample output
   bool stage;                // a group is scalar: shared-memory instruction staging buffers
+  int extra_smem = 0;        // extra dynamic shared memory per CTA (occupancy tuning)
+  int carveout = -1;         // preferred shared-memory carveout, percent (-1: driver default)
   cudaStream_t stream;
 };
 

@@ -51,67 +51,202 @@ struct Layout {
 
 __device__ __forceinline__ float act(float x) { return tanhf(x); }
 
-// Weights (BF16 on the device) -> FP32 in shared memory.
-__device__ void load_weights(const __nv_bfloat16 *wq, float *sw, int n) {
-  for (int i = threadIdx.x; i < n; i += blockDim.x) sw[i] = __bfloat162float(wq[i]);
+// ---------------------------------------------------------------------------------------
+// Tensor-core GEMM tiles (mma.sync m16n8k16, BF16 operands, FP32 accumulate).
+//
+// The weights are BF16 numbers, so a weight operand is exact in BF16.  Activations and
+// gradients are FP32: they enter as a two-term BF16 split x = hi + lo (hi = bf16(x),
+// lo = bf16(x - hi), about 16 significant bits), so a product with a weight operand is
+// A_hi*W + A_lo*W and a product of two FP32 operands is A_hi*B_hi + A_hi*B_lo + A_lo*B_hi.
+// Accumulation is FP32 throughout; every sum over samples runs in a fixed order.
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);   // .x (low half) = a
+  return *reinterpret_cast<uint32_t *>(&h);
 }
 
-// One block = WTILE samples: forward, weighted NLL, backward, per-block gradient sums
-// (one atomicAdd per parameter per block).
-__global__ void made_grad_kernel(const __nv_bfloat16 *__restrict__ wq, int D, float WALPHA,
-                                 const float *__restrict__ X, const float *__restrict__ wt, int n,
-                                 float *__restrict__ grad, float *__restrict__ loss) {
-  extern __shared__ float sm[];
+// (hi, lo) BF16 pairs of two FP32 values.
+__device__ __forceinline__ void split_bf16(float a, float b, uint32_t &hi, uint32_t &lo) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+  hi = *reinterpret_cast<uint32_t *>(&h);
+  lo = *reinterpret_cast<uint32_t *>(&l);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// One warp: C[16][8*NT] += A[16][16*kt] * B[16*kt][8*NT] over k tiles kt = 0 .. KT-1.
+// fa(r, k) gives A (FP32), fb(k, n) gives B; B_EXACT: B is BF16-exact (2 products per tile),
+// otherwise it is split as well (3 products).  Fragment layouts of m16n8k16 (PTX ISA): lane
+// l = 4g + t holds A rows g, g+8 at columns 2t, 2t+1, 2t+8, 2t+9; B columns n = g at rows 2t,
+// 2t+1, 2t+8, 2t+9; C rows g, g+8 at columns 2t, 2t+1.
+template <int NT, bool B_EXACT, typename FA, typename FB>
+__device__ __forceinline__ void warp_gemm(float (&c)[NT][4], int KT, FA fa, FB fb) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll 1
+  for (int kt = 0; kt < KT; ++kt) {
+    const int k0 = 16 * kt + 2 * t;
+    uint32_t ah[4], al[4];
+    split_bf16(fa(g, k0), fa(g, k0 + 1), ah[0], al[0]);
+    split_bf16(fa(g + 8, k0), fa(g + 8, k0 + 1), ah[1], al[1]);
+    split_bf16(fa(g, k0 + 8), fa(g, k0 + 9), ah[2], al[2]);
+    split_bf16(fa(g + 8, k0 + 8), fa(g + 8, k0 + 9), ah[3], al[3]);
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+      const int n = 8 * j + g;
+      if (B_EXACT) {
+        const uint32_t b0 = pack_bf16(fb(k0, n), fb(k0 + 1, n)), b1 = pack_bf16(fb(k0 + 8, n), fb(k0 + 9, n));
+        mma_bf16(c[j], ah, b0, b1);
+        mma_bf16(c[j], al, b0, b1);
+      } else {
+        uint32_t bh0, bl0, bh1, bl1;
+        split_bf16(fb(k0, n), fb(k0 + 1, n), bh0, bl0);
+        split_bf16(fb(k0 + 8, n), fb(k0 + 9, n), bh1, bl1);
+        mma_bf16(c[j], ah, bh0, bh1);
+        mma_bf16(c[j], ah, bl0, bl1);
+        mma_bf16(c[j], al, bh0, bh1);
+      }
+    }
+  }
+}
+
+template <int NT>
+__device__ __forceinline__ void zero_acc(float (&c)[NT][4]) {
+#pragma unroll
+  for (int j = 0; j < NT; ++j) c[j][0] = c[j][1] = c[j][2] = c[j][3] = 0.f;
+}
+
+// Store C (rows r0 + g, r0 + g + 8; columns 8j + 2t, +1) through f(r, n, value).
+template <int NT, typename F>
+__device__ __forceinline__ void store_acc(const float (&c)[NT][4], F f) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int j = 0; j < NT; ++j) {
+    const int n = 8 * j + 2 * t;
+    f(g, n, c[j][0]);
+    f(g, n + 1, c[j][1]);
+    f(g + 8, n, c[j][2]);
+    f(g + 8, n + 1, c[j][3]);
+  }
+}
+
+// Shared-memory image of the network for the tensor-core kernels: BF16 weights with the
+// first layer's inputs padded to 16 and the output rows padded to a multiple of 16 (zeros),
+// FP32 biases.
+template <int D>
+struct TcNet {
+  static constexpr int DK = D * WKP;
+  static constexpr int DKP = 16 * ((DK + 15) / 16);   // output rows, padded
+  static constexpr int HS = WH + 4;                   // FP32 activation row stride (floats)
+  static constexpr int DLS = DKP + 4;                 // FP32 logit row stride
+  static constexpr int KIN = 16;                      // first-layer inputs, padded
+  // bf16 offsets
+  static constexpr int W1 = 0, W2 = W1 + WH * KIN, W3 = W2 + WH * WH, W4 = W3 + WH * WH, NW = W4 + DKP * WH;
+  // float offsets of the biases
+  static constexpr int B1 = 0, B2 = B1 + WH, B3 = B2 + WH, B4 = B3 + WH, NB = B4 + DKP;
+};
+
+template <int D>
+__device__ void load_net(const __nv_bfloat16 *__restrict__ wq, __nv_bfloat16 *sw, float *sb) {
+  using N = TcNet<D>;
   const Layout L(D);
-  float *W = sm;                       // L.n
-  float *x = W + L.n;                  // [WTILE][WDMAX]
-  float *h1 = x + WTILE * WDMAX;       // [WTILE][WH]
-  float *h2 = h1 + WTILE * WH;
-  float *h3 = h2 + WTILE * WH;
-  float *dl = h3 + WTILE * WH;         // [WTILE][DK]
-  float *dB = dl + WTILE * L.DK;       // [WTILE][WH]
+  const __nv_bfloat16 z = __float2bfloat16(0.f);
+  for (int i = threadIdx.x; i < WH * N::KIN; i += blockDim.x) {
+    const int j = i / N::KIN, k = i % N::KIN;
+    sw[N::W1 + i] = k < D ? wq[L.oW1 + j * D + k] : z;
+  }
+  for (int i = threadIdx.x; i < WH * WH; i += blockDim.x) {
+    sw[N::W2 + i] = wq[L.oW2 + i];
+    sw[N::W3 + i] = wq[L.oW3 + i];
+  }
+  for (int i = threadIdx.x; i < N::DKP * WH; i += blockDim.x) sw[N::W4 + i] = i < N::DK * WH ? wq[L.oW4 + i] : z;
+  for (int i = threadIdx.x; i < WH; i += blockDim.x) {
+    sb[N::B1 + i] = __bfloat162float(wq[L.ob1 + i]);
+    sb[N::B2 + i] = __bfloat162float(wq[L.ob2 + i]);
+    sb[N::B3 + i] = __bfloat162float(wq[L.ob3 + i]);
+  }
+  for (int i = threadIdx.x; i < N::DKP; i += blockDim.x) sb[N::B4 + i] = i < N::DK ? __bfloat162float(wq[L.ob4 + i]) : 0.f;
+}
+
+// One hidden layer for the 16 rows of this warp: out[r][j] = act(b[j] + sum_k W[j][k] in[r][k]).
+template <int D>
+__device__ __forceinline__ void hidden_layer(const __nv_bfloat16 *w, int kin, const float *bias, const float *in,
+                                             int in_stride, float *out, int r0) {
+  using N = TcNet<D>;
+  float c[WH / 8][4];
+  zero_acc(c);
+  warp_gemm<WH / 8, true>(
+      c, kin / 16, [&](int r, int k) { return in[(r0 + r) * in_stride + k]; },
+      [&](int k, int n) { return __bfloat162float(w[n * kin + k]); });
+  store_acc(c, [&](int r, int n, float v) { out[(r0 + r) * N::HS + n] = act(v + bias[n]); });
+}
+
+template <int D>
+constexpr size_t tc_grad_smem() {
+  using N = TcNet<D>;
+  return sizeof(__nv_bfloat16) * N::NW + sizeof(float) * (N::NB + WTILE * N::KIN + 4 * WTILE * N::HS + WTILE * N::DLS);
+}
+
+// One block = WTILE (64) samples, 4 warps of 16 samples: forward, |f|-weighted negative
+// log-likelihood, backward.  The block's gradient and loss go to its own row of gpart / lpart
+// (summed over blocks in order by grad_reduce_kernel), so the result does not depend on
+// scheduling.
+template <int D>
+__global__ void __launch_bounds__(128) made_grad_tc_kernel(const __nv_bfloat16 *__restrict__ wq, float WALPHA,
+                                                           const float *__restrict__ X, const float *__restrict__ wt,
+                                                           int n, float *__restrict__ gpart,
+                                                           float *__restrict__ lpart) {
+  using N = TcNet<D>;
+  const Layout L(D);
+  extern __shared__ __align__(16) unsigned char tc_smem[];
+  __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(tc_smem);
+  float *sb = reinterpret_cast<float *>(sw + N::NW);
+  float *x = sb + N::NB;                 // [WTILE][KIN]
+  float *h1 = x + WTILE * N::KIN;        // [WTILE][HS]
+  float *h2 = h1 + WTILE * N::HS;
+  float *h3 = h2 + WTILE * N::HS;
+  float *dB = h3 + WTILE * N::HS;
+  float *dl = dB + WTILE * N::HS;        // [WTILE][DLS]
+  __shared__ float red[4];
   const int s0 = blockIdx.x * WTILE;
   const int ns = min(WTILE, n - s0);
-  load_weights(wq, W, L.n);
-  for (int i = threadIdx.x; i < WTILE * WDMAX; i += blockDim.x) {
-    const int s = i / WDMAX, d = i % WDMAX;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r0 = 16 * warp;
+  float *gp = gpart + (size_t)blockIdx.x * L.n;
+  load_net<D>(wq, sw, sb);
+  for (int i = threadIdx.x; i < WTILE * N::KIN; i += blockDim.x) {
+    const int s = i / N::KIN, d = i % N::KIN;
     x[i] = (s < ns && d < D) ? 2.f * X[(size_t)(s0 + s) * D + d] - 1.f : 0.f;
   }
   __syncthreads();
-  // forward
-  for (int i = threadIdx.x; i < WTILE * WH; i += blockDim.x) {
-    const int s = i / WH, j = i % WH;
-    float a = W[L.ob1 + j];
-    for (int k = 0; k < D; ++k) a = fmaf(W[L.oW1 + j * D + k], x[s * WDMAX + k], a);
-    h1[i] = act(a);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < WTILE * WH; i += blockDim.x) {
-    const int s = i / WH, j = i % WH;
-    float a = W[L.ob2 + j];
-    for (int k = 0; k < WH; ++k) a = fmaf(W[L.oW2 + j * WH + k], h1[s * WH + k], a);
-    h2[i] = act(a);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < WTILE * WH; i += blockDim.x) {
-    const int s = i / WH, j = i % WH;
-    float a = W[L.ob3 + j];
-    for (int k = 0; k < WH; ++k) a = fmaf(W[L.oW3 + j * WH + k], h2[s * WH + k], a);
-    h3[i] = act(a);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < WTILE * L.DK; i += blockDim.x) {
-    const int s = i / L.DK, o = i % L.DK;
-    float a = W[L.ob4 + o];
-    for (int k = 0; k < WH; ++k) a = fmaf(W[L.oW4 + o * WH + k], h3[s * WH + k], a);
-    dl[i] = a;
+  // forward (each warp its own 16 rows)
+  hidden_layer<D>(sw + N::W1, N::KIN, sb + N::B1, x, N::KIN, h1, r0);
+  __syncwarp();
+  hidden_layer<D>(sw + N::W2, WH, sb + N::B2, h1, N::HS, h2, r0);
+  __syncwarp();
+  hidden_layer<D>(sw + N::W3, WH, sb + N::B3, h2, N::HS, h3, r0);
+  __syncwarp();
+  {
+    float c[N::DKP / 8][4];
+    zero_acc(c);
+    warp_gemm<N::DKP / 8, true>(
+        c, WH / 16, [&](int r, int k) { return h3[(r0 + r) * N::HS + k]; },
+        [&](int k, int o) { return __bfloat162float(sw[N::W4 + o * WH + k]); });
+    store_acc(c, [&](int r, int o, float v) { dl[(r0 + r) * N::DLS + o] = v + sb[N::B4 + o]; });
   }
   __syncthreads();
   // loss and d loss / d logits, one thread per (sample, dimension)
   float lsum = 0.f;
   for (int i = threadIdx.x; i < WTILE * D; i += blockDim.x) {
     const int s = i / D, d = i % D;
-    float *lg = dl + s * L.DK + d * WKP;
+    float *lg = dl + s * N::DLS + d * WKP;
     if (s >= ns) {
       for (int c = 0; c < WKP; ++c) lg[c] = 0.f;
       continue;
@@ -122,7 +257,7 @@ __global__ void made_grad_kernel(const __nv_bfloat16 *__restrict__ wq, int D, fl
     for (int c = 0; c < WKP; ++c) a[c] = __expf(lg[c] - mx);
     for (int c = 0; c < WK; ++c) S += a[c] + a[c + 1];
     S *= 0.5f / WK;
-    const float xd = 0.5f * (x[s * WDMAX + d] + 1.f);
+    const float xd = 0.5f * (x[s * N::KIN + d] + 1.f);
     int b = (int)floorf(xd * WK);
     b = b < 0 ? 0 : (b > WK - 1 ? WK - 1 : b);
     const float t = xd * WK - (float)b;
@@ -138,77 +273,129 @@ __global__ void made_grad_kernel(const __nv_bfloat16 *__restrict__ wq, int D, fl
       lg[c] = k1 * a[c] * (own - k2 * nc);
     }
   }
-  atomicAdd(loss, lsum);
+  for (int i = threadIdx.x; i < WTILE * (N::DLS - N::DK); i += blockDim.x) {   // padded logit columns
+    const int s = i / (N::DLS - N::DK), o = N::DK + i % (N::DLS - N::DK);
+    dl[s * N::DLS + o] = 0.f;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+  if (lane == 0) red[warp] = lsum;
   __syncthreads();
-  // backward: W4, b4, dh3
-  for (int i = threadIdx.x; i < L.DK * WH; i += blockDim.x) {
-    const int o = i / WH, j = i % WH;
-    float g = 0.f;
-    for (int s = 0; s < ns; ++s) g = fmaf(dl[s * L.DK + o], h3[s * WH + j], g);
-    atomicAdd(grad + L.oW4 + i, g);
+  if (threadIdx.x == 0) lpart[blockIdx.x] = ((red[0] + red[1]) + red[2]) + red[3];
+  // dW4[o][j] = sum_s dl[s][o] h3[s][j]: m tiles of outputs over the warps, K = samples
+  for (int mt = warp; mt < N::DKP / 16; mt += 4) {
+    float c[WH / 8][4];
+    zero_acc(c);
+    warp_gemm<WH / 8, false>(
+        c, WTILE / 16, [&](int r, int k) { return dl[k * N::DLS + 16 * mt + r]; },
+        [&](int k, int j) { return h3[k * N::HS + j]; });
+    store_acc(c, [&](int r, int j, float v) {
+      const int o = 16 * mt + r;
+      if (o < N::DK) gp[L.oW4 + o * WH + j] = v;
+    });
   }
-  for (int o = threadIdx.x; o < L.DK; o += blockDim.x) {
+  for (int o = threadIdx.x; o < N::DK; o += blockDim.x) {
     float g = 0.f;
-    for (int s = 0; s < ns; ++s) g += dl[s * L.DK + o];
-    atomicAdd(grad + L.ob4 + o, g);
+    for (int s = 0; s < WTILE; ++s) g += dl[s * N::DLS + o];
+    gp[L.ob4 + o] = g;
   }
-  for (int i = threadIdx.x; i < WTILE * WH; i += blockDim.x) {
-    const int s = i / WH, j = i % WH;
-    float a = 0.f;
-    for (int o = 0; o < L.DK; ++o) a = fmaf(W[L.oW4 + o * WH + j], dl[s * L.DK + o], a);
-    dB[i] = a * (1.f - h3[i] * h3[i]);
+  // dh3 = dl W4 (own rows), dB = dh3 (1 - h3^2)
+  {
+    float c[WH / 8][4];
+    zero_acc(c);
+    warp_gemm<WH / 8, true>(
+        c, N::DKP / 16, [&](int r, int k) { return dl[(r0 + r) * N::DLS + k]; },
+        [&](int k, int j) { return __bfloat162float(sw[N::W4 + k * WH + j]); });
+    store_acc(c, [&](int r, int j, float v) {
+      const float h = h3[(r0 + r) * N::HS + j];
+      dB[(r0 + r) * N::HS + j] = v * (1.f - h * h);
+    });
   }
   __syncthreads();
-  // W3, b3, dh2 (into h3)
-  for (int i = threadIdx.x; i < WH * WH; i += blockDim.x) {
-    const int jo = i / WH, ji = i % WH;
-    float g = 0.f;
-    for (int s = 0; s < ns; ++s) g = fmaf(dB[s * WH + jo], h2[s * WH + ji], g);
-    atomicAdd(grad + L.oW3 + i, g);
+  // dW3 = dB^T h2, db3; then dh2 = dB W3 -> h3 (own rows), times (1 - h2^2)
+  {
+    float c[WH / 8][4];
+    zero_acc(c);
+    warp_gemm<WH / 8, false>(
+        c, WTILE / 16, [&](int r, int k) { return dB[k * N::HS + r0 + r]; },
+        [&](int k, int j) { return h2[k * N::HS + j]; });
+    store_acc(c, [&](int r, int j, float v) { gp[L.oW3 + (r0 + r) * WH + j] = v; });
   }
   for (int j = threadIdx.x; j < WH; j += blockDim.x) {
     float g = 0.f;
-    for (int s = 0; s < ns; ++s) g += dB[s * WH + j];
-    atomicAdd(grad + L.ob3 + j, g);
+    for (int s = 0; s < WTILE; ++s) g += dB[s * N::HS + j];
+    gp[L.ob3 + j] = g;
   }
-  for (int i = threadIdx.x; i < WTILE * WH; i += blockDim.x) {
-    const int s = i / WH, j = i % WH;
-    float a = 0.f;
-    for (int o = 0; o < WH; ++o) a = fmaf(W[L.oW3 + o * WH + j], dB[s * WH + o], a);
-    h3[i] = a * (1.f - h2[i] * h2[i]);
+  {
+    float c[WH / 8][4];
+    zero_acc(c);
+    warp_gemm<WH / 8, true>(
+        c, WH / 16, [&](int r, int k) { return dB[(r0 + r) * N::HS + k]; },
+        [&](int k, int j) { return __bfloat162float(sw[N::W3 + k * WH + j]); });
+    store_acc(c, [&](int r, int j, float v) {
+      const float h = h2[(r0 + r) * N::HS + j];
+      h3[(r0 + r) * N::HS + j] = v * (1.f - h * h);
+    });
   }
   __syncthreads();
-  // W2, b2, dh1 (into dB)
-  for (int i = threadIdx.x; i < WH * WH; i += blockDim.x) {
-    const int jo = i / WH, ji = i % WH;
-    float g = 0.f;
-    for (int s = 0; s < ns; ++s) g = fmaf(h3[s * WH + jo], h1[s * WH + ji], g);
-    atomicAdd(grad + L.oW2 + i, g);
+  // dW2 = h3^T h1, db2; then dh1 = h3 W2 -> dB (own rows), times (1 - h1^2)
+  {
+    float c[WH / 8][4];
+    zero_acc(c);
+    warp_gemm<WH / 8, false>(
+        c, WTILE / 16, [&](int r, int k) { return h3[k * N::HS + r0 + r]; },
+        [&](int k, int j) { return h1[k * N::HS + j]; });
+    store_acc(c, [&](int r, int j, float v) { gp[L.oW2 + (r0 + r) * WH + j] = v; });
   }
   for (int j = threadIdx.x; j < WH; j += blockDim.x) {
     float g = 0.f;
-    for (int s = 0; s < ns; ++s) g += h3[s * WH + j];
-    atomicAdd(grad + L.ob2 + j, g);
+    for (int s = 0; s < WTILE; ++s) g += h3[s * N::HS + j];
+    gp[L.ob2 + j] = g;
+  }
+  __syncthreads();   // every warp has read dB above before it is overwritten
+  {
+    float c[WH / 8][4];
+    zero_acc(c);
+    warp_gemm<WH / 8, true>(
+        c, WH / 16, [&](int r, int k) { return h3[(r0 + r) * N::HS + k]; },
+        [&](int k, int j) { return __bfloat162float(sw[N::W2 + k * WH + j]); });
+    store_acc(c, [&](int r, int j, float v) {
+      const float h = h1[(r0 + r) * N::HS + j];
+      dB[(r0 + r) * N::HS + j] = v * (1.f - h * h);
+    });
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < WTILE * WH; i += blockDim.x) {
-    const int s = i / WH, j = i % WH;
-    float a = 0.f;
-    for (int o = 0; o < WH; ++o) a = fmaf(W[L.oW2 + o * WH + j], h3[s * WH + o], a);
-    dB[i] = a * (1.f - h1[i] * h1[i]);
-  }
-  __syncthreads();
-  // W1, b1
-  for (int i = threadIdx.x; i < WH * D; i += blockDim.x) {
-    const int jo = i / D, k = i % D;
-    float g = 0.f;
-    for (int s = 0; s < ns; ++s) g = fmaf(dB[s * WH + jo], x[s * WDMAX + k], g);
-    atomicAdd(grad + L.oW1 + i, g);
+  // dW1 = dB^T x (inputs padded to 8 columns), db1
+  {
+    float c[1][4];
+    zero_acc(c);
+    warp_gemm<1, false>(
+        c, WTILE / 16, [&](int r, int k) { return dB[k * N::HS + r0 + r]; },
+        [&](int k, int d) { return x[k * N::KIN + d]; });
+    store_acc(c, [&](int r, int d, float v) {
+      if (d < D) gp[L.oW1 + (r0 + r) * D + d] = v;
+    });
   }
   for (int j = threadIdx.x; j < WH; j += blockDim.x) {
     float g = 0.f;
-    for (int s = 0; s < ns; ++s) g += dB[s * WH + j];
-    atomicAdd(grad + L.ob1 + j, g);
+    for (int s = 0; s < WTILE; ++s) g += dB[s * N::HS + j];
+    gp[L.ob1 + j] = g;
+  }
+}
+
+// grad[i] = sum over blocks b (in order) of gpart[b][i]; loss likewise.
+__global__ void grad_reduce_kernel(const float *__restrict__ gpart, const float *__restrict__ lpart, int nb, int np,
+                                   float *__restrict__ grad, float *__restrict__ loss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < np) {
+    float g = 0.f;
+    for (int b = 0; b < nb; ++b) g += gpart[(size_t)b * np + i];
+    grad[i] = g;
+  }
+  if (i == 0) {
+    float l = 0.f;
+    for (int b = 0; b < nb; ++b) l += lpart[b];
+    *loss = l;
   }
 }
 
@@ -227,76 +414,103 @@ __global__ void adam_kernel(float *p, float *m, float *v, const float *g, const 
   }
 }
 
-// y (Sobol) -> x = w(y) and the importance weight 1/q(x); one thread per sample.
-__global__ void warp_map_kernel(const __nv_bfloat16 *__restrict__ wq, int D, float WALPHA,
-                                const uint32_t *__restrict__ sm_m,
-                                const uint32_t *__restrict__ sm_x0, uint64_t first, uint64_t n,
-                                double *__restrict__ pts) {
-  extern __shared__ float sw[];
-  const Layout L(D);
-  load_weights(wq, sw, L.n);
+template <int D>
+constexpr size_t tc_map_smem() {
+  using N = TcNet<D>;
+  return sizeof(__nv_bfloat16) * N::NW + sizeof(float) * (N::NB + WTILE * N::KIN + 2 * WTILE * N::HS + WTILE * 24);
+}
+
+// y (Sobol) -> x = w(y) and the importance weight 1/q(x).  A block maps WTILE (64) samples,
+// 4 warps of 16; for each dimension d in turn a warp runs the network on its 16 samples (the
+// inputs x_<d found so far, x_>=d still zero, which the masks ignore), keeps the 17 logits of
+// dimension d and inverts that dimension's CDF, one lane per sample.
+template <int D>
+__global__ void __launch_bounds__(128) warp_map_tc_kernel(const __nv_bfloat16 *__restrict__ wq, float WALPHA,
+                                                          const uint32_t *__restrict__ sm_m,
+                                                          const uint32_t *__restrict__ sm_x0, uint64_t first,
+                                                          uint64_t n, double *__restrict__ pts) {
+  using N = TcNet<D>;
+  extern __shared__ __align__(16) unsigned char tc_smem[];
+  __nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(tc_smem);
+  float *sb = reinterpret_cast<float *>(sw + N::NW);
+  float *xin = sb + N::NB;               // [WTILE][KIN]
+  float *ha = xin + WTILE * N::KIN;      // [WTILE][HS]
+  float *hb = ha + WTILE * N::HS;
+  float *lg = hb + WTILE * N::HS;        // [WTILE][24]
+  load_net<D>(wq, sw, sb);
+  for (int i = threadIdx.x; i < WTILE * N::KIN; i += blockDim.x) xin[i] = 0.f;
   __syncthreads();
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint64_t idx = first + i;
-  const uint32_t gray = (uint32_t)(idx ^ (idx >> 1));
-  float y[WDMAX], xin[WDMAX];
-  for (int d = 0; d < D; ++d) {
-    uint32_t v = sm_x0[d];
-    for (int b = 0; b < 32; ++b)
-      if ((gray >> b) & 1u) v ^= sm_m[d * 32 + b];
-    y[d] = (float)ldexp((double)v, -32);
-    xin[d] = 0.f;
-  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r0 = 16 * warp;
+  const uint64_t base = (uint64_t)blockIdx.x * WTILE + r0;   // this warp's first sample
+  const bool mine = lane < 16 && base + lane < n;             // lane r handles sample base + r
+  float y[D];
   double wt = 1.0;
-  float h1[WH], h2[WH], h3[WH];
-  for (int d = 0; d < D; ++d) {
-    for (int j = 0; j < WH; ++j) {
-      float a = sw[L.ob1 + j];
-      for (int k = 0; k < D; ++k) a = fmaf(sw[L.oW1 + j * D + k], xin[k], a);
-      h1[j] = act(a);
+  if (mine) {
+    const uint64_t idx = first + base + lane;
+    const uint32_t gray = (uint32_t)(idx ^ (idx >> 1));
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      uint32_t v = sm_x0[d];
+      for (int b = 0; b < 32; ++b)
+        if ((gray >> b) & 1u) v ^= sm_m[d * 32 + b];
+      y[d] = (float)ldexp((double)v, -32);
     }
-    for (int j = 0; j < WH; ++j) {
-      float a = sw[L.ob2 + j];
-      for (int k = 0; k < WH; ++k) a = fmaf(sw[L.oW2 + j * WH + k], h1[k], a);
-      h2[j] = act(a);
-    }
-    for (int j = 0; j < WH; ++j) {
-      float a = sw[L.ob3 + j];
-      for (int k = 0; k < WH; ++k) a = fmaf(sw[L.oW3 + j * WH + k], h2[k], a);
-      h3[j] = act(a);
-    }
-    float v[WKP], mx = -1e30f;
-    for (int c = 0; c < WKP; ++c) {
-      const int o = d * WKP + c;
-      float a = sw[L.ob4 + o];
-      for (int k = 0; k < WH; ++k) a = fmaf(sw[L.oW4 + o * WH + k], h3[k], a);
-      v[c] = a;
-      mx = fmaxf(mx, a);
-    }
-    float S = 0.f;
-    for (int c = 0; c < WKP; ++c) v[c] = __expf(v[c] - mx);
-    for (int c = 0; c < WK; ++c) S += v[c] + v[c + 1];
-    S *= 0.5f / WK;
-    for (int c = 0; c < WKP; ++c) v[c] = (1.f - WALPHA) * v[c] / S + WALPHA;
-    // invert the quadratic CDF: bin mass m_b = (v_b + v_{b+1}) / 2K
-    float cum = 0.f;
-    int b = WK - 1;
-    for (int c = 0; c < WK; ++c) {
-      const float mb = 0.5f * (v[c] + v[c + 1]) / WK;
-      if (y[d] < cum + mb || c == WK - 1) { b = c; break; }
-      cum += mb;
-    }
-    const float r = fmaxf(y[d] - cum, 0.f) * WK;
-    const float dv = v[b + 1] - v[b];
-    float t = 2.f * r / (v[b] + sqrtf(fmaxf(v[b] * v[b] + 2.f * dv * r, 0.f)));
-    t = t < 0.f ? 0.f : (t >= 1.f ? 0.99999994f : t);
-    const float xd = ((float)b + t) / (float)WK;
-    xin[d] = 2.f * xd - 1.f;
-    pts[i * (D + 1) + d] = (double)xd;
-    wt /= (double)(v[b] + dv * t);
   }
-  pts[i * (D + 1) + D] = wt;
+#pragma unroll 1
+  for (int d = 0; d < D; ++d) {
+    hidden_layer<D>(sw + N::W1, N::KIN, sb + N::B1, xin, N::KIN, ha, r0);
+    __syncwarp();
+    hidden_layer<D>(sw + N::W2, WH, sb + N::B2, ha, N::HS, hb, r0);
+    __syncwarp();
+    hidden_layer<D>(sw + N::W3, WH, sb + N::B3, hb, N::HS, ha, r0);
+    __syncwarp();
+    {
+      float c[3][4];   // the 17 logits of dimension d (24 columns)
+      zero_acc(c);
+      const int o0 = d * WKP;
+      warp_gemm<3, true>(
+          c, WH / 16, [&](int r, int k) { return ha[(r0 + r) * N::HS + k]; },
+          [&](int k, int o) { return __bfloat162float(sw[N::W4 + (o0 + o) * WH + k]); });
+      store_acc(c, [&](int r, int o, float v) { lg[(r0 + r) * 24 + o] = v + sb[N::B4 + o0 + o]; });
+    }
+    __syncwarp();
+    if (mine) {
+      float v[WKP], mx = -1e30f;
+      const float *l = lg + (r0 + lane) * 24;
+      for (int c = 0; c < WKP; ++c) {
+        v[c] = l[c];
+        mx = fmaxf(mx, v[c]);
+      }
+      float S = 0.f;
+      for (int c = 0; c < WKP; ++c) v[c] = __expf(v[c] - mx);
+      for (int c = 0; c < WK; ++c) S += v[c] + v[c + 1];
+      S *= 0.5f / WK;
+      for (int c = 0; c < WKP; ++c) v[c] = (1.f - WALPHA) * v[c] / S + WALPHA;
+      // invert the quadratic CDF: bin mass m_b = (v_b + v_{b+1}) / 2K
+      float yd = 0.f;
+#pragma unroll
+      for (int e = 0; e < D; ++e)
+        if (e == d) yd = y[e];
+      float cum = 0.f;
+      int b = WK - 1;
+      for (int c = 0; c < WK; ++c) {
+        const float mb = 0.5f * (v[c] + v[c + 1]) / WK;
+        if (yd < cum + mb || c == WK - 1) { b = c; break; }
+        cum += mb;
+      }
+      const float r = fmaxf(yd - cum, 0.f) * WK;
+      const float dv = v[b + 1] - v[b];
+      float t = 2.f * r / (v[b] + sqrtf(fmaxf(v[b] * v[b] + 2.f * dv * r, 0.f)));
+      t = t < 0.f ? 0.f : (t >= 1.f ? 0.99999994f : t);
+      const float xd = ((float)b + t) / (float)WK;
+      xin[(r0 + lane) * N::KIN + d] = 2.f * xd - 1.f;
+      pts[(base + lane) * (D + 1) + d] = (double)xd;
+      wt /= (double)(v[b] + dv * t);
+    }
+    __syncwarp();
+  }
+  if (mine) pts[(base + lane) * (D + 1) + D] = wt;
 }
 
 }  // namespace
@@ -307,6 +521,7 @@ struct WarpRec {
   DevBuf<float> p, m, v, g, mask, loss;
   DevBuf<__nv_bfloat16> wq;
   DevBuf<float> X, w;
+  DevBuf<float> gpart, lpart;   // per-block gradient and loss rows of made_grad_tc_kernel
   int64_t t = 0;
   std::vector<float> hmask;
 };
@@ -314,7 +529,7 @@ struct WarpRec {
 void destroy_warps(qiw_ctx *c) {
   for (WarpRec *w : c->warps) {
     w->p.release(); w->m.release(); w->v.release(); w->g.release(); w->mask.release(); w->loss.release();
-    w->wq.release(); w->X.release(); w->w.release();
+    w->wq.release(); w->X.release(); w->w.release(); w->gpart.release(); w->lpart.release();
     delete w;
   }
   c->warps.clear();
@@ -322,20 +537,34 @@ void destroy_warps(qiw_ctx *c) {
 
 int warp_dim(qiw_ctx *c, int id) { return c->warps[id]->D; }
 
-static size_t train_smem(int D) {
-  Layout L(D);
-  return sizeof(float) * ((size_t)L.n + WTILE * WDMAX + 4 * WTILE * WH + (size_t)WTILE * L.DK);
-}
+// Launch of a D-templated warp kernel for the runtime dimension (2 <= D <= WDMAX).
+#define QIW_WARP_D_SWITCH(D, CALL) \
+  switch (D) {                     \
+    case 2: CALL(2); break;        \
+    case 3: CALL(3); break;        \
+    case 4: CALL(4); break;        \
+    case 5: CALL(5); break;        \
+    case 6: CALL(6); break;        \
+    case 7: CALL(7); break;        \
+    default: CALL(8); break;       \
+  }
 
 int warp_map_device(qiw_ctx *c, int id, const uint32_t *m_dev, const uint32_t *x0_dev, uint64_t first, uint64_t n,
                     double *pts_dev) {
   WarpRec *w = c->warps[id];
-  const size_t smem = sizeof(float) * Layout(w->D).n;
-  cudaFuncSetAttribute(warp_map_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  const int threads = 128;
-  const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+  const unsigned blocks = (unsigned)((n + WTILE - 1) / WTILE);
   if (blocks == 0) return QIW_OK;
-  warp_map_kernel<<<blocks, threads, smem, c->stream>>>(w->wq.p, w->D, w->alpha, m_dev, x0_dev, first, n, pts_dev);
+  cudaError_t e = cudaSuccess;
+#define QIW_MAP_CALL(DD)                                                                                   \
+  {                                                                                                        \
+    const size_t smem = tc_map_smem<DD>();                                                                 \
+    e = cudaFuncSetAttribute(warp_map_tc_kernel<DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e == cudaSuccess)                                                                                  \
+      warp_map_tc_kernel<DD><<<blocks, 128, smem, c->stream>>>(w->wq.p, w->alpha, m_dev, x0_dev, first, n, pts_dev); \
+  }
+  QIW_WARP_D_SWITCH(w->D, QIW_MAP_CALL)
+#undef QIW_MAP_CALL
+  if (e != cudaSuccess) return c->cuda(e, "warp map kernel: shared memory");
   return c->cuda(cudaGetLastError(), "warp map kernel");
 }
 
@@ -455,17 +684,30 @@ static int upload_batch(qiw_ctx *c, WarpRec *w, const double *x, const double *w
   return QIW_OK;
 }
 
+// Gradient and loss of n samples into w->g and w->loss: one made_grad_tc_kernel block per 64
+// samples writes its own row, grad_reduce_kernel sums the rows in block order.
 static int run_grad(qiw_ctx *c, WarpRec *w, const float *X, const float *wt, int64_t n) {
   const int Lw = Layout(w->D).n;
-  const size_t smem = train_smem(w->D);
-  cudaFuncSetAttribute(made_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  int rc;
-  if ((rc = c->cuda(cudaMemsetAsync(w->g.p, 0, sizeof(float) * Lw, c->stream), "warp grad")) ||
-      (rc = c->cuda(cudaMemsetAsync(w->loss.p, 0, sizeof(float), c->stream), "warp grad")))
-    return rc;
   const unsigned blocks = (unsigned)((n + WTILE - 1) / WTILE);
-  made_grad_kernel<<<blocks, 128, smem, c->stream>>>(w->wq.p, w->D, w->alpha, X, wt, (int)n, w->g.p, w->loss.p);
-  return c->cuda(cudaGetLastError(), "warp grad kernel");
+  int rc;
+  if ((rc = c->cuda(w->gpart.reserve((size_t)blocks * Lw), "warp grad partials")) ||
+      (rc = c->cuda(w->lpart.reserve(blocks), "warp grad partials")))
+    return rc;
+  cudaError_t e = cudaSuccess;
+#define QIW_GRAD_CALL(DD)                                                                                    \
+  {                                                                                                          \
+    const size_t smem = tc_grad_smem<DD>();                                                                  \
+    e = cudaFuncSetAttribute(made_grad_tc_kernel<DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e == cudaSuccess)                                                                                    \
+      made_grad_tc_kernel<DD><<<blocks, 128, smem, c->stream>>>(w->wq.p, w->alpha, X, wt, (int)n, w->gpart.p, w->lpart.p); \
+  }
+  QIW_WARP_D_SWITCH(w->D, QIW_GRAD_CALL)
+#undef QIW_GRAD_CALL
+  if (e != cudaSuccess) return c->cuda(e, "warp grad kernel: shared memory");
+  if ((rc = c->cuda(cudaGetLastError(), "warp grad kernel"))) return rc;
+  grad_reduce_kernel<<<(Lw + 255) / 256, 256, 0, c->stream>>>(w->gpart.p, w->lpart.p, (int)blocks, Lw, w->g.p,
+                                                              w->loss.p);
+  return c->cuda(cudaGetLastError(), "warp grad reduce kernel");
 }
 
 int qiw_warp_grad(qiw_ctx *c, int32_t id, const double *x, const double *wt, int64_t n, double *grad_out,
