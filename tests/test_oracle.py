@@ -126,6 +126,32 @@ def test_oracle_reproduces_reference_golden_inchworm():
     assert np.linalg.norm(g - want) <= 1e-6 * np.linalg.norm(want)
 
 
+def test_golden_inchworm_residual_is_bounded_per_step():
+    """Where the oracle departs from test/inchworm.h5, and by how much per step.
+
+    The final P of inchworm! carries every later normalize!(P, tau) factor exp(-tau_j lambda_n)
+    (src/inchworm.jl:488).  Taking out one common factor exp(-tau_j dL), dL fitted on the bare
+    point tau_1 (whose raw value is bit-exact), leaves the shape of P: it matches the fixture to
+    rounding through the first bold step (tau_2) and departs by ~2e-10 at the second (tau_3),
+    growing about quadratically with the step index after that -- a deviation of the order of
+    1e-10 in each step's integral (source not identified: the incremental-spline P lookups are
+    ruled out, they depart by 1e-5 already at the first bold step).  The reference checks its
+    own run against this fixture only to Julia's default isapprox tolerance, sqrt(eps) = 1.5e-8
+    in norm (test/inchworm.jl:45-51)."""
+    gold = _load("inchworm_h5.json")
+    exp = models.single_level()
+    pb = orc.inchworm(exp, range(0, 4), range(0, 3), 2 ** 8)
+    taus = np.array([exp.grid.tau(j) for j in range(exp.grid.n_tau)])
+    r = [pb.P_data[s][:, 0, 0] / (np.array(gold["P"][s]["re"]) + 1j * np.array(gold["P"][s]["im"])) for s in range(2)]
+    dL = -np.log(r[0][1].real) / taus[1]
+    assert abs(dL) < 2e-8                                   # the accumulated normalisation drift
+    for s in range(2):
+        shape = np.abs(r[s] * np.exp(taus * dL) - 1)
+        assert shape[:3].max() < 1e-14                      # bare step and first bold step
+        assert shape[3] < 5e-10                             # second bold step
+        assert shape.max() < 2e-7
+
+
 def test_oracle_reproduces_reference_golden_diff_inchworm():
     """test/inchworm.jl:214-239 (diff_inchworm!, orders 0:3, N = 2^8) via test/inchworm.h5."""
     gold = _load("inchworm_h5.json")
