@@ -350,11 +350,39 @@ def _traffic(args):
     return None
 
 
+def bare_step(ses, exp, kmax, N_total, prec, comm):
+    """The bench's bare step tau_0 -> tau_1 (orders 0:kmax), written into exp.P."""
+    from qiw import _lib, ppgf
+    from qiw.diagrammatics import get_topologies_at_order
+    from qiw.inchworm import TopologiesInputData, _accumulate
+    grid = exp.grid
+    bare = [TopologiesInputData(o, 2 * o, get_topologies_at_order(o), N_total) for o in range(0, kmax + 1)]
+    val, _, _ = _accumulate(ses.run(_lib.QIW_GROUP_BARE, bare, grid.tau(0), 0.0, grid.tau(1), prec, comm), bare,
+                            exp.dims)
+    ppgf.set_ppgf(exp.P, 1, val)
+
+
+def make_step(ses, exp, tds, prec, comm):
+    """One bench step n: inch step tau_n -> tau_{n+1} of every group (each rank its sample range,
+    one all-reduce per launch through comm), set_ppgf! and normalize!(P, tau) on the host."""
+    from qiw import _lib, ppgf
+    from qiw.inchworm import _accumulate
+    grid = exp.grid
+
+    def step(n):
+        ses.dev.set_ppgf(exp.P)
+        res = ses.run(_lib.QIW_GROUP_BOLD, tds, grid.tau(0), grid.tau(n), grid.tau(n + 1), prec, comm)
+        v, _, _ = _accumulate(res, tds, exp.dims)
+        ppgf.set_ppgf(exp.P, n + 1, v)
+        ppgf.normalize_tau(exp.P, n + 1)
+    return step
+
+
 def run_ours(args):
     import torch
-    from qiw import _lib, ppgf
+    from qiw import _lib
     from qiw.device import Device
-    from qiw.inchworm import _Session, _accumulate, Comm, TorchComm
+    from qiw.inchworm import _Session, Comm, TorchComm
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -378,22 +406,10 @@ def run_ours(args):
     units_rank = sum(len(td.topologies) * (N if td.order > 0 else 1) for td in tds if td.order > 0)
     flops_rank = sum(stats[id(td)].flops_per_sample * N for td in tds if td.order > 0)
     # bare step, then warm-up and timed regular steps
-    from qiw.inchworm import TopologiesInputData
-    from qiw.diagrammatics import get_topologies_at_order
-    bare = [TopologiesInputData(o, 2 * o, get_topologies_at_order(o), N * world) for o in range(0, kmax + 1)]
-    val, _, _ = _accumulate(ses.run(_lib.QIW_GROUP_BARE, bare, grid.tau(0), 0.0, grid.tau(1), prec, comm), bare,
-                            exp.dims)
-    ppgf.set_ppgf(exp.P, 1, val)
+    bare_step(ses, exp, kmax, N * world, prec, comm)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     kernel_ms, wall_s = [], []
-    h2d = d2h = 0
-
-    def step(n):
-        dev.set_ppgf(exp.P)
-        res = ses.run(_lib.QIW_GROUP_BOLD, tds, grid.tau(0), grid.tau(n), grid.tau(n + 1), prec, comm)
-        v, _, _ = _accumulate(res, tds, exp.dims)
-        ppgf.set_ppgf(exp.P, n + 1, v)
-        ppgf.normalize_tau(exp.P, n + 1)
+    step = make_step(ses, exp, tds, prec, comm)
 
     n = 1
     for _ in range(args.warmup):
@@ -722,8 +738,17 @@ def run_batch(args):
     from qiw.batch import Batch
     from qiw.device import Device
     from qiw.inchworm import inchworm
+    from qiw.batch import shard_solves, solve_cost
     prec = _lib.QIW_PREC_FP32 if args.precision == "fp32" else _lib.QIW_PREC_FP64
-    specs = batch_solves(args.seed, args.solves)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:   # independent solves: each rank runs its share whole, no data exchange
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    specs_all = batch_solves(args.seed, args.solves)
+    mine = shard_solves([solve_cost(p["n_tau"], p["kmax"], p["N"]) for p in specs_all], rank, world)
+    specs = [specs_all[i] for i in mine]
     mk = lambda p: models.anderson(eps=p["eps"], U=p["U"], D=2.0, V=p["V"], beta=p["beta"], n_tau=p["n_tau"])
     exps = [mk(p) for p in specs]
     t0 = time.perf_counter()
@@ -742,21 +767,32 @@ def run_batch(args):
         P_batch = [b.P_table(i) for i in range(len(exps))]
         runs.append((r, time.perf_counter() - t0))
     r, wall = min(runs, key=lambda x: x[0].kernel_ms)
+    kernel_s, samples = r.kernel_ms * 1e-3, r.topology_samples
+    if world > 1:   # whole job: every rank's samples over the slowest rank's time
+        import torch.distributed as dist
+        t = torch.tensor([kernel_s, wall], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        u = torch.tensor([samples], dtype=torch.float64)
+        dist.all_reduce(u)
+        kernel_s, wall, samples = float(t[0]), float(t[1]), float(u[0])
+        if rank != 0:
+            return
     direct = b.run(prec, graph=False, autotune=True) if args.direct else None
     line = {"mode": "batch", "metric": "topology-sample evaluations per second, independent Anderson solves",
-            "value": r.topology_samples / (r.kernel_ms * 1e-3), "unit": "topology-samples/s", "n_gpus": 1,
-            "steps": len(runs), "ms_per_step": r.kernel_ms, "higher_is_better": True, "dtype": args.precision.replace("fp", "f"),
-            "data": "synthetic", "config": {"workload": f"{len(specs)} Anderson solves, seed {args.seed}",
+            "value": samples / kernel_s, "unit": "topology-samples/s", "n_gpus": world, "scaling": "strong",
+            "steps": len(runs), "ms_per_step": kernel_s * 1e3, "higher_is_better": True, "dtype": args.precision.replace("fp", "f"),
+            "data": "synthetic", "config": {"workload": f"{len(specs_all)} Anderson solves, seed {args.seed}",
                                             "ranges": "beta U[2,40], n_tau U{64..512}, U U[0.5,4], eps U[-1,1], V U[0.2,1], D=2, max order U{2..6}, N 2^U{8..14}",
-                                            "total_steps": int(sum(p["n_tau"] - 1 for p in specs))},
-            "e2e": {"value": r.topology_samples / wall, "unit": "topology-samples/s", "seconds": wall},
-            "flops": r.flops, "tflops": r.flops / (r.kernel_ms * 1e-3) / 1e12,
+                                            "total_steps": int(sum(p["n_tau"] - 1 for p in specs_all))},
+            "e2e": {"value": samples / wall, "unit": "topology-samples/s", "seconds": wall},
+            "solves_on_rank0": len(specs),
+            "flops_rank0": r.flops, "tflops_rank0": r.flops / (r.kernel_ms * 1e-3) / 1e12,
             "tiles": {"threads": r.threads, "persistent": r.persistent, "grid": r.grid, "tiles_per_step": r.tiles_per_step,
                       "autotune_ms_step1": {f"{t}{'p' if pm == 0 else '1'}": round(first.tune_ms[i * 2 + pm], 3)
                                             for i, t in enumerate((32, 64, 128)) for pm in (0, 1)}},
             "graph_nodes": r.graph_nodes, "n_plans": r.n_plans, "setup_s": setup_s, "first_run_s": first_s,
             "direct_launches_ms": direct.kernel_ms if direct else None}
-    if not args.no_sequential:
+    if not args.no_sequential and world == 1:
         dev = Device(int(os.environ.get("LOCAL_RANK", "0")))
         seq_s, worst = 0.0, 0.0
         for i, p in enumerate(specs):

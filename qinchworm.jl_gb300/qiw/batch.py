@@ -10,6 +10,7 @@ one CUDA graph.  Solves may differ in model parameters, grids, orders and sample
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass
 from typing import List, Optional, Sequence, Union
 
@@ -126,6 +127,30 @@ class Batch:
             blk = flat[o:o + n_tau * d * d].reshape(n_tau, d, d)   # [tau][l][k], k fastest
             P_s.data[...] = np.transpose(blk, (0, 2, 1))
             o += n_tau * d * d
+
+
+def solve_cost(n_tau: int, max_order: int, N_samples: int) -> float:
+    """Relative cost of one solve for sharding: steps x samples x bold topologies per step
+    (sum over orders k <= max_order of (2k - 1)!! topologies, each counted once per n_pts_after
+    group it falls in is close enough for balancing)."""
+    tops = sum(math.prod(range(2 * k - 1, 0, -2)) if k > 0 else 1 for k in range(max_order + 1))
+    return float(max(n_tau - 1, 1)) * N_samples * tops
+
+
+def shard_solves(costs: Sequence[float], rank: int, size: int) -> List[int]:
+    """Indices of the solves rank `rank` of `size` runs: independent solves need no exchange, so
+    they are dealt out whole (longest first, each to the rank with the least cost so far; ties to
+    the lowest rank).  Every rank computes the same assignment from the same costs."""
+    if size < 1 or not 0 <= rank < size:
+        raise ValueError("rank must lie in 0..size-1")
+    load = [0.0] * size
+    mine: List[int] = []
+    for i in sorted(range(len(costs)), key=lambda j: (-costs[j], j)):
+        r = min(range(size), key=lambda q: (load[q], q))
+        load[r] += costs[i]
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
 
 
 def inchworm_batch(expansions: Sequence, orders: Union[Sequence[int], Sequence[Sequence[int]]],

@@ -206,3 +206,82 @@ def test_two_rank_inchworm_equals_single_rank():
         for r in (0, 1):
             got = res[r][s]
             assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+
+
+def _bench_steps(comm=None, n_steps=3):
+    """bench.py's bare step and regular steps (bench.bare_step / bench.make_step) on a small
+    Anderson model through OracleDevice; returns the P tables afterwards."""
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import bench
+    from qiw import models, _lib
+    from qiw.inchworm import Comm, _Session
+    exp = models.anderson(n_tau=8)
+    comm = comm or Comm()
+    tds = bench.bold_groups(range(0, 3), 32)   # N_samples * world: each of two ranks takes 16
+    ses = _Session(OracleDevice(), exp)
+    bench.bare_step(ses, exp, 2, 32, _lib.QIW_PREC_FP64, comm)
+    step = bench.make_step(ses, exp, tds, _lib.QIW_PREC_FP64, comm)
+    for n in range(1, 1 + n_steps):
+        step(n)
+    return [P_s.data.copy() for P_s in exp.P]
+
+
+def _worker_bench(rank, world, port, q):
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for p in (os.path.join(root, "qinchworm.jl_gb300"), os.path.join(root, "oracle"), os.path.join(root, "tests")):
+        sys.path.insert(0, p)
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from qiw.inchworm import TorchComm
+    from test_multirank import _bench_steps
+    q.put((rank, _bench_steps(TorchComm())))
+    dist.destroy_process_group()
+
+
+def test_two_rank_bench_steps_equal_single_rank():
+    """bench.py's torchrun path (weak scaling: each rank a sample range of every group, one
+    all-reduce per launch) gives the single-rank P on two gloo ranks."""
+    res = _run_ranks(_worker_bench)
+    want = _bench_steps()
+    for r in (0, 1):
+        for a, b in zip(res[r], want):
+            assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
+
+
+def _worker_shard(rank, world, port, q):
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for p in (os.path.join(root, "qinchworm.jl_gb300"), root):
+        sys.path.insert(0, p)
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    from qiw.batch import shard_solves, solve_cost
+    specs = bench.batch_solves(2024, 64)
+    costs = [solve_cost(p["n_tau"], p["kmax"], p["N"]) for p in specs]
+    mine = shard_solves(costs, rank, world)
+    shares = [None] * world
+    dist.all_gather_object(shares, mine)
+    q.put((rank, (shares, costs)))
+    dist.destroy_process_group()
+
+
+def test_batch_solves_shard_over_ranks_without_exchange():
+    """The 64 seed-drawn solves of the batch benchmark dealt out whole over gloo ranks: every
+    rank computes the same partition on its own (no exchange), the shares are disjoint, cover
+    every solve, and no rank carries more than the even share plus the largest single solve."""
+    for world in (2, 3):
+        res = _run_ranks(_worker_shard, world)
+        shares, costs = res[0]
+        for r in range(1, world):
+            assert res[r][0] == shares
+        flat = sorted(i for s in shares for i in s)
+        assert flat == list(range(len(costs)))
+        loads = [sum(costs[i] for i in s) for s in shares]
+        assert max(loads) <= sum(costs) / world + max(costs)
