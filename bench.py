@@ -212,7 +212,7 @@ def parity_check(dev, ses, exp, tds, t, prec, slices):
             "oracle_s": time.perf_counter() - t0}
 
 
-def time_to_tol(dev, step=200, n_loop=256, tols=(1e-3, 1e-4), n_ref=2 ** 20, n_max=2 ** 16):
+def time_to_tol(dev, step=200, n_loop=256, tols=(1e-3, 1e-4), n_ref=2 ** 20, n_max=2 ** 18):
     """Time to a target error on one late eg inch step: warped FP32 (learned warps fitted on the
     step's groups, fit time included) against plain FP64, errors max|sum of the step's groups -
     reference| / max|reference|, reference = plain FP64 at n_ref samples per group.  P comes from

@@ -355,8 +355,9 @@ int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
       delete g;
       return c->fail(QIW_ERR_MEMORY, "qiw_group_create: per-sample arena above the largest kernel instantiation");
     }
-    // flag bits: 0 = (c != 1), 1 = (c == -1)
-    for (Instr &I : g->plan.ins) I.flags = (uint8_t)((I.c != 1.0 ? 1 : 0) | (I.c == -1.0 ? 2 : 0));
+    // flag bits: 0 = (c != 1), 1 = (c == -1); bits 2-4 come from the planner
+    for (Instr &I : g->plan.ins)
+      I.flags = (uint8_t)((I.flags & ~3u) | (I.c != 1.0 ? 1 : 0) | (I.c == -1.0 ? 2 : 0));
     plan_store_insert(std::move(key), g->plan);
   }
   // the FP32 copy holds c rounded to float in the low 4 bytes of c

@@ -46,6 +46,14 @@ __device__ __forceinline__ Instr load_instr(const Instr *p) {
   return I;
 }
 
+// Register copy of a P multiply's product for the out-edges that follow it: blocks of at most
+// kRegTmp elements (dims 1, 2, 4).  Instruction flag bits set by the planner: 2 = the source is
+// the register copy, 3 = keep the product in registers, 4 = skip the product's arena store.
+constexpr int kRegTmp = 16;
+#ifndef QIW_REG_PRODUCTS
+#define QIW_REG_PRODUCTS 1
+#endif
+
 // Dynamic shared memory of the evaluation kernels: the reduction rows [warps][RESMAX] doubles,
 // then (launches with scalar programs) two instruction chunks of blockDim.x entries.
 extern __shared__ __align__(16) unsigned char qiw_dyn_smem[];
@@ -117,6 +125,31 @@ __device__ __forceinline__ void pmul_u(T *A, int dst, int pm, int src) {
     }
 }
 
+// The same product kept in registers t[] for the out-edges that follow it (flag bit 3); the
+// arena copy is written unless no later instruction reads it (flag bit 4).  Same roundings.
+template <typename T, int R, int C>
+__device__ __forceinline__ void pmul_r(T *A, T (&t)[kRegTmp], int dst, int pm, int src, bool store) {
+  static_assert(R * C <= kRegTmp, "register product");
+  T p[R * R], x[R * C];
+#pragma unroll
+  for (int i = 0; i < R * R; ++i) p[i] = A[pm + i];
+#pragma unroll
+  for (int i = 0; i < R * C; ++i) x[i] = A[src + i];
+#pragma unroll
+  for (int j = 0; j < C; ++j)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      T acc = p[r] * x[j * R];
+#pragma unroll
+      for (int k = 1; k < R; ++k) acc = fmaT<T>(p[k * R + r], x[j * R + k], acc);
+      t[j * R + r] = acc;
+    }
+  if (store) {
+#pragma unroll
+    for (int i = 0; i < R * C; ++i) A[dst + i] = t[i];
+  }
+}
+
 template <typename T, int R, int C>
 __device__ __forceinline__ void pmuld_u(T *A, int dst, int pm, int src) {
   T p[R], x[R * C];
@@ -132,13 +165,15 @@ __device__ __forceinline__ void pmuld_u(T *A, int dst, int pm, int src) {
 
 // dst (=|+=) coef * O * src.  MODE 0: no coefficient (coef == 1 exactly), MODE 1: the
 // coefficient scales the smaller of src (K x C) and the product (R x C).
-template <typename T, int R, int K, int C, int MODE>
-__device__ __forceinline__ void omul_m(T *A, const T *O, int dst, int oa, int src, T coef, bool accf) {
+// XR: src is the register copy t[] of the preceding P multiply (flag bit 2), not the arena.
+template <typename T, int R, int K, int C, int MODE, bool XR>
+__device__ __forceinline__ void omul_m(T *A, const T *O, int dst, int oa, int src, T coef, bool accf,
+                                       const T (&t)[kRegTmp]) {
   T o[R * K], x[K * C];
 #pragma unroll
   for (int i = 0; i < R * K; ++i) o[i] = __ldg(O + oa + i);
 #pragma unroll
-  for (int i = 0; i < K * C; ++i) x[i] = A[src + i];
+  for (int i = 0; i < K * C; ++i) x[i] = XR ? t[i] : A[src + i];
   constexpr bool scale_src = (MODE == 1) && (K < R);
   if (scale_src) {
 #pragma unroll
@@ -167,16 +202,26 @@ __device__ __forceinline__ void omul_m(T *A, const T *O, int dst, int oa, int sr
 
 template <typename T, int R, int K, int C>
 __device__ __forceinline__ void omul_u(T *A, const T *O, int dst, int oa, int src, T coef, bool accf,
-                                       bool has_coef) {
-  if (has_coef) omul_m<T, R, K, C, 1>(A, O, dst, oa, src, coef, accf);
-  else omul_m<T, R, K, C, 0>(A, O, dst, oa, src, coef, accf);
+                                       bool has_coef, const T (&t)[kRegTmp]) {
+  if (has_coef) omul_m<T, R, K, C, 1, false>(A, O, dst, oa, src, coef, accf, t);
+  else omul_m<T, R, K, C, 0, false>(A, O, dst, oa, src, coef, accf, t);
 }
 
-template <typename T, int N>
-__device__ __forceinline__ void axpy_u(T *A, int dst, int src, T coef, bool accf, bool has_coef) {
+template <typename T, int R, int K, int C>
+__device__ __forceinline__ void omul_ur(T *A, const T *O, int dst, int oa, int src, T coef, bool accf,
+                                        bool has_coef, const T (&t)[kRegTmp]) {
+  if constexpr (K * C <= kRegTmp) {
+    if (has_coef) omul_m<T, R, K, C, 1, true>(A, O, dst, oa, src, coef, accf, t);
+    else omul_m<T, R, K, C, 0, true>(A, O, dst, oa, src, coef, accf, t);
+  }
+}
+
+template <typename T, int N, bool XR>
+__device__ __forceinline__ void axpy_u(T *A, int dst, int src, T coef, bool accf, bool has_coef,
+                                       const T (&t)[kRegTmp]) {
   T x[N];
 #pragma unroll
-  for (int i = 0; i < N; ++i) x[i] = A[src + i];
+  for (int i = 0; i < N; ++i) x[i] = XR ? t[i] : A[src + i];
   if (has_coef) {
 #pragma unroll
     for (int i = 0; i < N; ++i) A[dst + i] = accf ? fmaT<T>(coef, x[i], A[dst + i]) : coef * x[i];
@@ -295,7 +340,10 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
 }
 
 template <typename T, int RESMAX>
-__device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, double *R) {
+__device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, double *R, T (&t)[kRegTmp]) {
+  // Register-held products in the FP32 kernels; the FP64 kernels (DFMA-bound, and at the
+  // register budget of their launch bound) ignore flag bits 2-4 and keep every product in the arena.
+  constexpr bool REG = QIW_REG_PRODUCTS && sizeof(T) == 4;
   const int rows = I.rows, cols = I.cols;
   switch (I.op) {
     case OP_LOADP: {  // c == 1 copies (x * 1 is exact)
@@ -330,7 +378,11 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
     }
     case OP_PMUL: {
       const int cr = dcode(rows), cc = dcode(cols);
-      if (cr >= 0 && cc >= 0) {
+      if (REG && (I.flags & 8u)) {   // dims 1, 2, 4 by construction (planner)
+        const int code = cr * 3 + cc;
+        const bool store = (I.flags & 16u) == 0;
+        QIW_D2(pmul_r, A, t, I.dst, I.a, I.src, store)
+      } else if (cr >= 0 && cc >= 0) {
         const int code = cr * 3 + cc;
         QIW_D2(pmul_u, A, I.dst, I.a, I.src)
       } else {
@@ -364,9 +416,12 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
       const bool has_coef = (I.w >= 0) || has_c(I);
       const T coef = edge_coef<T>(I, A);
       const int cr = dcode(rows), ck = dcode(inner), cc = dcode(cols);
-      if (cr >= 0 && ck >= 0 && cc >= 0) {
+      if (REG && (I.flags & 4u)) {   // source in registers: dims 1, 2, 4 by construction (planner)
         const int code = cr * 9 + ck * 3 + cc;
-        QIW_D3(omul_u, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef)
+        QIW_D3(omul_ur, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef, t)
+      } else if (cr >= 0 && ck >= 0 && cc >= 0) {
+        const int code = cr * 9 + ck * 3 + cc;
+        QIW_D3(omul_u, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef, t)
       } else {
 #pragma unroll 1
         for (int j = 0; j < cols; ++j)
@@ -386,12 +441,22 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
       const T coef = edge_coef<T>(I, A);
       const int n = rows * cols;
       const bool accf = I.acc != 0;
+      if (REG && (I.flags & 4u)) {   // source in registers (n in 1, 2, 4, 8, 16 by construction)
+        switch (n) {
+          case 1: axpy_u<T, 1, true>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+          case 2: axpy_u<T, 2, true>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+          case 4: axpy_u<T, 4, true>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+          case 8: axpy_u<T, 8, true>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+          default: axpy_u<T, 16, true>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+        }
+        break;
+      }
       switch (n) {
-        case 1: axpy_u<T, 1>(A, I.dst, I.src, coef, accf, has_coef); break;
-        case 2: axpy_u<T, 2>(A, I.dst, I.src, coef, accf, has_coef); break;
-        case 4: axpy_u<T, 4>(A, I.dst, I.src, coef, accf, has_coef); break;
-        case 8: axpy_u<T, 8>(A, I.dst, I.src, coef, accf, has_coef); break;
-        case 16: axpy_u<T, 16>(A, I.dst, I.src, coef, accf, has_coef); break;
+        case 1: axpy_u<T, 1, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+        case 2: axpy_u<T, 2, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+        case 4: axpy_u<T, 4, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+        case 8: axpy_u<T, 8, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+        case 16: axpy_u<T, 16, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
         default:
 #pragma unroll 1
           for (int e = 0; e < n; ++e) {
@@ -578,6 +643,9 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
   bool active = sidx < w.n_samples;   // cleared for samples a domain map discards
   double wt = 1.0;
   T A[ARENA];
+  T tr[kRegTmp];   // register copy of the last P multiply's product (flag bits 2-4)
+#pragma unroll
+  for (int i = 0; i < kRegTmp; ++i) tr[i] = (T)0;
   double R[RESMAX];
 #pragma unroll 1
   for (int e = 0; e < res_size; ++e) R[e] = 0.0;
@@ -620,7 +688,7 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
 #pragma unroll 1
       for (int ip = i0; ip < i1; ++ip) {
         const Instr I = load_instr(ins + ip);
-        exec_instr<T, RESMAX>(I, A, O, R);
+        exec_instr<T, RESMAX>(I, A, O, R, tr);
       }
     }
   }
@@ -657,7 +725,7 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
 }
 
 template <typename T, int ARENA, int RESMAX, bool EXTRAS>
-__global__ void __launch_bounds__(kMaxThreads, kMinBlocks)
+__global__ void __launch_bounds__(kMaxThreads, sizeof(T) == 4 ? kMinBlocks32 : kMinBlocks)
     eval_kernel(DevProblem pb, const DevGroup *__restrict__ groups, const DevWork *__restrict__ works,
                 const int4 *__restrict__ cta_map, double *__restrict__ partials) {
   const int4 cm = cta_map[blockIdx.x];   // (work item, batch, first sample of the tile, partial row)

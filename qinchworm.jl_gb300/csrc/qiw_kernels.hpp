@@ -13,6 +13,10 @@ constexpr int kMaxThreads = 128;     // samples per CTA (upper bound)
 #define QIW_MIN_BLOCKS 5
 #endif
 constexpr int kMinBlocks = QIW_MIN_BLOCKS;  // 128-thread blocks per SM: FP64 at 94 registers, no spills
+#ifndef QIW_MIN_BLOCKS_FP32
+#define QIW_MIN_BLOCKS_FP32 5
+#endif
+constexpr int kMinBlocks32 = QIW_MIN_BLOCKS_FP32;  // the same bound for the FP32 kernels
 constexpr int kArenaSmall = 1024;    // per-sample arena instantiations (elements)
 constexpr int kArenaLarge = 8192;
 constexpr int kArenaHuge = 20480;   // large-sector problems (9x9 blocks); results always kResLarge

@@ -32,6 +32,14 @@ namespace {
 
 enum PosKind { PK_VAR = 0, PK_IDENT = 1, PK_OPER = 2 };
 
+// Instruction flag bits set by the planner (bits 0-1 are set on upload from the coefficient):
+// the product of a P multiply whose blocks have dimensions 1, 2 or 4 stays in registers for the
+// out-edges emitted right after it.
+constexpr uint8_t kFlagSrcReg = 4;    // OMUL / AXPY: the source is the register copy
+constexpr uint8_t kFlagKeepReg = 8;   // PMUL: keep the product in registers
+constexpr uint8_t kFlagNoStore = 16;  // PMUL: no instruction reads the product's arena copy
+inline bool small_dim(int d) { return d == 1 || d == 2 || d == 4; }
+
 struct Layout {
   int n = 0;
   std::vector<int> kind, op;     // per position
@@ -399,6 +407,7 @@ struct Builder {
       }
       int64_t tmp = (zero_iv && !ident_root) ? -1 : al.alloc((int64_t)d * d0);
       bool diagP = (g.kind == QIW_GROUP_BARE);
+      int64_t pmul_at = -1;   // index of this node's P multiply when its product may stay in registers
       if (ident_root && zero_iv) {
         Instr I = mk(OP_LOADI);
         I.rows = (uint8_t)d;
@@ -441,9 +450,10 @@ struct Builder {
           ins.push_back(I);
           fl += diagP ? (double)d * d0 : 2.0 * d * d * d0;
           al.release(src, (int64_t)d * d0);
+          if (!diagP && !all_scalar && small_dim(d) && small_dim(d0)) pmul_at = (int64_t)ins.size() - 1;
         }
       }
-      bool tmp_taken = false;
+      bool tmp_taken = false, tmp_read = false;   // the arena copy of tmp is needed / read
       ready.clear();
       for (int e = nu.out_begin; e < nu.out_begin + nu.out_count; ++e) {
         const DEdge &E = edges[e];
@@ -453,6 +463,7 @@ struct Builder {
         if (E.op < 0 && E.w < 0 && n_out_alive[u] == 1 && pending[v] == 1 && slot[v] < 0) {
           slot[v] = tmp;  // alias: V_v is tmp itself
           tmp_taken = true;
+          tmp_read = true;
         } else {
           bool acc = slot[v] >= 0;
           if (!acc) slot[v] = al.alloc(dsz(v));
@@ -468,6 +479,8 @@ struct Builder {
             I.src = (int32_t)tmp;
             I.w = E.w;
             I.c = (E.op < 0) ? 1.0 : sc;
+            if (pmul_at >= 0 && small_dim(dv)) I.flags |= kFlagSrcReg;
+            else tmp_read = true;
             ins.push_back(I);
             fl += (double)dv * d0 * ((E.w >= 0 || I.c != 1.0 ? 1 : 0) + (acc ? 1 : 0));
           } else {
@@ -480,11 +493,17 @@ struct Builder {
             I.src = (int32_t)tmp;
             I.a = (int32_t)pb.op_valoff[(size_t)E.op * pb.S + nu.s];
             I.w = E.w;
+            if (pmul_at >= 0 && small_dim(dv)) I.flags |= kFlagSrcReg;
+            else tmp_read = true;
             ins.push_back(I);
             fl += 2.0 * dv * d * d0 + (E.w >= 0 ? (double)dv * d0 : 0.0);
           }
         }
         if (--pending[v] == 0) ready.push_back(v);
+      }
+      if (pmul_at >= 0) {   // the out-edges above read the product from registers
+        ins[pmul_at].flags |= kFlagKeepReg;
+        if (!tmp_read) ins[pmul_at].flags |= kFlagNoStore;
       }
       if (!tmp_taken) al.release(tmp, (int64_t)d * d0);
       for (auto it = ready.rbegin(); it != ready.rend(); ++it) stack.push_back(*it);
