@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--samples", type=int, default=1024)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "fp32tc"],
+                    help="fp32tc: FP32 chains with the 9-wide operator multiplies on tensor cores (t2g)")
     ap.add_argument("--model", default="eg", choices=["eg", "anderson", "t2g", "anderson_b40"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the GPU-vs-oracle check of the benchmarked step")
@@ -261,12 +262,18 @@ def time_to_tol(dev, step=200, n_loop=256, tols=(1e-3, 1e-4), n_ref=2 ** 20, n_m
     ref_w, _ = total(n_ref, _lib.QIW_PREC_FP32, True)
     sc = float(np.abs(ref).max())
     ref_err = float(np.abs(ref - ref_w).max()) / sc
+    def first_point(N):   # the first Sobol point alone (x = 0: every time on its segment's lower end), weight 1/N
+        works = [Work(gid, *t, 0, 1, N) for (o, gid) in gids if o > 0]
+        res = dev.integrate(works, _lib.QIW_PREC_FP64)
+        return np.concatenate([sum(r[s_] for r in res).ravel() for s_ in range(len(res[0]))])
+
     sweep, N = [], 2 ** 8
     while N <= n_max:
         vp, sp = total(N, _lib.QIW_PREC_FP64, False)
         vw, sw = total(N, _lib.QIW_PREC_FP32, True)
         sweep.append({"N": N, "err_plain_fp64": float(np.abs(vp - ref).max()) / sc, "s_plain_fp64": sp,
-                      "err_warped_fp32": float(np.abs(vw - ref).max()) / sc, "s_warped_fp32": sw})
+                      "err_warped_fp32": float(np.abs(vw - ref).max()) / sc, "s_warped_fp32": sw,
+                      "err_plain_fp64_without_first_point": float(np.abs(vp - first_point(N) - ref).max()) / sc})
         N *= 2
     out = {"workload": "eg Kanamori U=2 J=0.2 beta=8 n_tau=256, orders 0:4, inch step tau_w index %d" % step,
            "reference": f"plain FP64, {n_ref} samples per group ({ref_s:.1f} s)", "reference_err": ref_err,
@@ -392,7 +399,7 @@ def run_ours(args):
         dist.init_process_group("gloo")
         comm = TorchComm()
     torch.cuda.set_device(local)
-    prec = _lib.QIW_PREC_FP32 if args.precision == "fp32" else _lib.QIW_PREC_FP64
+    prec = {"fp64": _lib.QIW_PREC_FP64, "fp32": _lib.QIW_PREC_FP32, "fp32tc": _lib.QIW_PREC_FP32_TC}[args.precision]
     exp, desc, kmax = workload(args.model)
     grid = exp.grid
     # weak scaling: every rank evaluates N_samples per group; the step result is all-reduced

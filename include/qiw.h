@@ -48,6 +48,8 @@ extern "C" {
 /* arithmetic of the chain products */
 #define QIW_PREC_FP64 0        /* plain FP64 throughout */
 #define QIW_PREC_FP32 1        /* FP32 chain products, FP64 compensated accumulation of qMC sums */
+#define QIW_PREC_FP32_TC 2     /* QIW_PREC_FP32 with the operator multiplies of 9-wide sector blocks on
+                                  tensor cores (mma.sync TF32, 3xTF32 split; large-block problems only) */
 
 typedef struct qiw_ctx qiw_ctx;
 

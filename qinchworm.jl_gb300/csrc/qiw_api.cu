@@ -134,7 +134,7 @@ int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
 }
 
 int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, LaunchTables *t) {
-  if (precision != QIW_PREC_FP64 && precision != QIW_PREC_FP32)
+  if (precision != QIW_PREC_FP64 && precision != QIW_PREC_FP32 && precision != QIW_PREC_FP32_TC)
     return c->fail(QIW_ERR_ARG, "qiw_integrate: unknown precision");
   if (!c->has_problem) return c->fail(QIW_ERR_ARG, "qiw_integrate: no problem set");
   bool need_P = false;
@@ -246,7 +246,7 @@ int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const De
                   double *partials, int *err, double *out) {
   const int n_cta = (int)t.cta_map.size();
   LaunchArgs la;
-  la.pb = c->dev_problem(precision == QIW_PREC_FP32);
+  la.pb = c->dev_problem(precision != QIW_PREC_FP64);
   la.groups = groups;
   la.works = works;
   la.cta_map = cta_map;
@@ -257,7 +257,8 @@ int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const De
   la.carveout = c->eval_carveout;
   la.arena_max = t.arena_max;
   la.res_max = t.res_max;
-  la.fp32 = precision == QIW_PREC_FP32;
+  la.fp32 = precision != QIW_PREC_FP64;
+  la.tc_omul = precision == QIW_PREC_FP32_TC;
   la.extras = false;
   la.stage = false;
   for (const DevWork &w : t.works) {
@@ -676,7 +677,7 @@ int qiw_measure_fma_peak(qiw_ctx *c, int32_t precision, double *tflops) {
   DevBuf<double> out;
   int rc;
   if ((rc = c->cuda(out.reserve((size_t)blocks * threads), "alloc"))) return rc;
-  const bool fp32 = precision == QIW_PREC_FP32;
+  const bool fp32 = precision != QIW_PREC_FP64;
   double best = 0.0;
   for (int rep = 0; rep < 4; ++rep) {
     if ((rc = c->cuda(cudaEventRecord(c->ev0, c->stream), "event")) ||

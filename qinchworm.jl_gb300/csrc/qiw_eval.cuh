@@ -53,6 +53,9 @@ constexpr int kRegTmp = 16;
 #ifndef QIW_REG_PRODUCTS
 #define QIW_REG_PRODUCTS 1
 #endif
+#ifndef QIW_BLOCK3
+#define QIW_BLOCK3 1
+#endif
 
 // Dynamic shared memory of the evaluation kernels: the reduction rows [warps][RESMAX] doubles,
 // then (launches with scalar programs) two instruction chunks of blockDim.x entries.
@@ -231,6 +234,158 @@ __device__ __forceinline__ void axpy_u(T *A, int dst, int src, T coef, bool accf
   }
 }
 
+// Products whose row count is a multiple of 3 (sector dimensions 3 and 9, the t2g model): three
+// rows of the left factor are held in registers and every column of the right factor is read
+// once per row block, instead of one left and one right arena load per multiply-add.  The sums
+// run over k in the same order from zero as the plain loops, so the results are identical.
+// LEFT_O: the left factor is an operator block (read-only table) instead of an arena block.
+template <typename T, bool LEFT_O>
+__device__ __forceinline__ void mul_rows3(T *A, const T *O, int dst, int la, int src, int rows, int inner,
+                                          int cols, T coef, bool scale, bool accf) {
+  constexpr int KB = 9;   // inner dimension held per pass
+#pragma unroll 1
+  for (int r0 = 0; r0 < rows; r0 += 3) {
+#pragma unroll 1
+    for (int k0 = 0; k0 < inner; k0 += KB) {
+      const int kn = min(KB, inner - k0);
+      T l0[KB], l1[KB], l2[KB];
+#pragma unroll
+      for (int k = 0; k < KB; ++k) {
+        if (k < kn) {
+          const int e = la + (k0 + k) * rows + r0;
+          l0[k] = LEFT_O ? __ldg(O + e) : A[e];
+          l1[k] = LEFT_O ? __ldg(O + e + 1) : A[e + 1];
+          l2[k] = LEFT_O ? __ldg(O + e + 2) : A[e + 2];
+        }
+      }
+#pragma unroll 1
+      for (int j = 0; j < cols; ++j) {
+        const int o = dst + j * rows + r0;
+        T a0, a1, a2;
+        if (k0 == 0) {
+          a0 = (T)0; a1 = (T)0; a2 = (T)0;
+        } else {   // partial sums of the previous pass (kept in the destination)
+          a0 = A[o]; a1 = A[o + 1]; a2 = A[o + 2];
+        }
+#pragma unroll
+        for (int k = 0; k < KB; ++k) {
+          if (k < kn) {
+            const T x = A[src + j * inner + k0 + k];
+            a0 = fmaT<T>(l0[k], x, a0);
+            a1 = fmaT<T>(l1[k], x, a1);
+            a2 = fmaT<T>(l2[k], x, a2);
+          }
+        }
+        if (k0 + KB < inner) {   // more passes: keep the raw partial sums
+          A[o] = a0; A[o + 1] = a1; A[o + 2] = a2;
+        } else if (!scale) {
+          A[o] = a0; A[o + 1] = a1; A[o + 2] = a2;
+        } else {
+          A[o] = accf ? fmaT<T>(coef, a0, A[o]) : coef * a0;
+          A[o + 1] = accf ? fmaT<T>(coef, a1, A[o + 1]) : coef * a1;
+          A[o + 2] = accf ? fmaT<T>(coef, a2, A[o + 2]) : coef * a2;
+        }
+      }
+    }
+  }
+}
+
+// Tensor-core operator multiply of the large-block FP32 kernels (sector dimension 9 in the
+// inner index; opt-in, DevProblem::tc_stage > 0).  All 32 samples of a warp apply the same
+// operator block O (rows x 9) to their own blocks X_s (9 x cols): per output column j that is
+// one GEMM Y[:, (s, j)] = O . X[:, (s, j)] over the warp's samples, run as mma.sync m16n8k8 TF32
+// (M = rows padded to 16, K = 9 padded to 16, N = 32 samples in 4 tiles of 8) with the 3xTF32
+// split a = a_hi + a_lo (a_hi = tf32(a), a_lo = tf32(a - a_hi); products a_hi b_hi + a_hi b_lo +
+// a_lo b_hi, FP32 accumulation).  The samples' blocks are staged in the warp's shared-memory
+// area [32][9 * cols]; column j of the results overwrites column j of the staged blocks once
+// every lane has read it.  Every lane of the warp must execute this (the kernel runs the
+// program on all lanes when tc_stage > 0).  Fragment layouts (PTX ISA, m16n8k8 .tf32): lane
+// 4g + t holds A[g][t], A[g+8][t], A[g][t+4], A[g+8][t+4]; B[t][g], B[t+4][g]; C[g][2t],
+// C[g][2t+1], C[g+8][2t], C[g+8][2t+1].
+constexpr int kTcK = 9, kTcMaxCols = 9, kTcWarpFloats = 32 * kTcK * kTcMaxCols;
+
+__device__ __forceinline__ uint32_t tf32_bits(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ void tf32_split(float x, uint32_t &hi, uint32_t &lo) {
+  hi = tf32_bits(x);
+  lo = tf32_bits(x - __uint_as_float(hi));
+}
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+static __device__ __noinline__ void omul_tc(float *A, const float *O, float *X, int dst, int oa, int src, int rows,
+                                        int cols, float coef, bool accf) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int KC = kTcK * cols;
+#pragma unroll 1
+  for (int i = 0; i < KC; ++i) X[lane * KC + i] = A[src + i];
+  uint32_t ah[2][4], al[2][4];
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks) {
+    const int k0 = 8 * ks + t, k1 = k0 + 4;
+    const float v0 = (g < rows && k0 < kTcK) ? __ldg(O + oa + k0 * rows + g) : 0.f;
+    const float v1 = (g + 8 < rows && k0 < kTcK) ? __ldg(O + oa + k0 * rows + g + 8) : 0.f;
+    const float v2 = (g < rows && k1 < kTcK) ? __ldg(O + oa + k1 * rows + g) : 0.f;
+    const float v3 = (g + 8 < rows && k1 < kTcK) ? __ldg(O + oa + k1 * rows + g + 8) : 0.f;
+    tf32_split(v0, ah[ks][0], al[ks][0]);
+    tf32_split(v1, ah[ks][1], al[ks][1]);
+    tf32_split(v2, ah[ks][2], al[ks][2]);
+    tf32_split(v3, ah[ks][3], al[ks][3]);
+  }
+  __syncwarp();
+#pragma unroll 1
+  for (int j = 0; j < cols; ++j) {
+    float c[4][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) c[q][0] = c[q][1] = c[q][2] = c[q][3] = 0.f;
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+      const int k0 = 8 * ks + t, k1 = k0 + 4;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float *xs = X + (8 * q + g) * KC + j * kTcK;
+        uint32_t bh0, bl0, bh1, bl1;
+        tf32_split(k0 < kTcK ? xs[k0] : 0.f, bh0, bl0);
+        tf32_split(k1 < kTcK ? xs[k1] : 0.f, bh1, bl1);
+        mma_tf32(c[q], ah[ks], bh0, bh1);
+        mma_tf32(c[q], ah[ks], bl0, bl1);
+        mma_tf32(c[q], al[ks], bh0, bh1);
+      }
+    }
+    __syncwarp();   // column j of every sample has been read
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int s0 = 8 * q + 2 * t;
+      if (g < rows) {
+        X[s0 * KC + j * kTcK + g] = c[q][0];
+        X[(s0 + 1) * KC + j * kTcK + g] = c[q][1];
+      }
+      if (g + 8 < rows) {
+        X[s0 * KC + j * kTcK + g + 8] = c[q][2];
+        X[(s0 + 1) * KC + j * kTcK + g + 8] = c[q][3];
+      }
+    }
+  }
+  __syncwarp();
+#pragma unroll 1
+  for (int j = 0; j < cols; ++j)
+#pragma unroll 1
+    for (int r = 0; r < rows; ++r) {
+      const float y = X[lane * KC + j * kTcK + r];
+      const int o = dst + j * rows + r;
+      A[o] = accf ? fmaf(coef, y, A[o]) : coef * y;
+    }
+  __syncwarp();   // the staging area is reused by the next instruction
+}
+
 #define QIW_D3(F, ...)                                                                            \
   switch (code) {                                                                                 \
     case 0: F<T, 1, 1, 1>(__VA_ARGS__); break;  case 1: F<T, 1, 1, 2>(__VA_ARGS__); break;        \
@@ -339,11 +494,16 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
   }
 }
 
-template <typename T, int RESMAX>
-__device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, double *R, T (&t)[kRegTmp]) {
-  // Register-held products in the FP32 kernels; the FP64 kernels (DFMA-bound, and at the
-  // register budget of their launch bound) ignore flag bits 2-4 and keep every product in the arena.
-  constexpr bool REG = QIW_REG_PRODUCTS && sizeof(T) == 4;
+// LARGE: the instantiation for problems with large sector blocks (the largest arena class, e.g.
+// t2g's 9 x 9 blocks), whose products take the 3-row register blocking; the others keep products
+// of dims 1, 2, 4 in registers.  Both only in the FP32 kernels: the FP64 kernels are DFMA-bound
+// and at the register budget of their launch bound, so they ignore flag bits 2-4 and keep
+// every product in the arena.  (One register budget cannot hold both paths without spills.)
+template <typename T, int RESMAX, bool LARGE>
+__device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, double *R, T (&t)[kRegTmp],
+                                           float *tcx) {
+  constexpr bool REG = QIW_REG_PRODUCTS && sizeof(T) == 4 && !LARGE;
+  constexpr bool BLOCK3 = QIW_BLOCK3 && sizeof(T) == 4 && LARGE;
   const int rows = I.rows, cols = I.cols;
   switch (I.op) {
     case OP_LOADP: {  // c == 1 copies (x * 1 is exact)
@@ -385,6 +545,8 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
       } else if (cr >= 0 && cc >= 0) {
         const int code = cr * 3 + cc;
         QIW_D2(pmul_u, A, I.dst, I.a, I.src)
+      } else if (BLOCK3 && rows % 3 == 0 && rows <= 9) {
+        mul_rows3<T, false>(A, O, I.dst, I.a, I.src, rows, rows, cols, (T)1, false, false);
       } else {
 #pragma unroll 1
         for (int j = 0; j < cols; ++j)
@@ -422,6 +584,10 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
       } else if (cr >= 0 && ck >= 0 && cc >= 0) {
         const int code = cr * 9 + ck * 3 + cc;
         QIW_D3(omul_u, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef, t)
+      } else if (BLOCK3 && tcx && inner == kTcK && rows <= 16 && cols <= kTcMaxCols) {
+        if constexpr (BLOCK3) omul_tc(A, O, tcx, I.dst, I.a, I.src, rows, cols, coef, I.acc != 0);
+      } else if (BLOCK3 && rows % 3 == 0 && inner <= 9 && !(I.acc && I.dst == I.src)) {
+        mul_rows3<T, true>(A, O, I.dst, I.a, I.src, rows, inner, cols, coef, true, I.acc != 0);
       } else {
 #pragma unroll 1
         for (int j = 0; j < cols; ++j)
@@ -643,6 +809,10 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
   bool active = sidx < w.n_samples;   // cleared for samples a domain map discards
   double wt = 1.0;
   T A[ARENA];
+  // this warp's tensor-core staging area (FP32 large-block kernels, opt-in), else null
+  float *tcx = (sizeof(T) == 4 && ARENA >= kArenaHuge && pb.tc_stage > 0)
+                   ? reinterpret_cast<float *>(qiw_dyn_smem + pb.tc_stage) + (threadIdx.x >> 5) * kTcWarpFloats
+                   : nullptr;
   T tr[kRegTmp];   // register copy of the last P multiply's product (flag bits 2-4)
 #pragma unroll
   for (int i = 0; i < kRegTmp; ++i) tr[i] = (T)0;
@@ -684,11 +854,15 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
         __syncthreads();     // the buffer is refilled two chunks later
       }
       cp_async_wait_0();
-    } else if (active) {
+    } else if (active || tcx) {   // with tensor-core multiplies every lane runs the program
 #pragma unroll 1
       for (int ip = i0; ip < i1; ++ip) {
         const Instr I = load_instr(ins + ip);
-        exec_instr<T, RESMAX>(I, A, O, R, tr);
+        exec_instr<T, RESMAX, (ARENA >= kArenaHuge)>(I, A, O, R, tr, tcx);
+      }
+      if (!active) {   // a lane without a sample ran the program on an unset arena: no result
+#pragma unroll 1
+        for (int e = 0; e < res_size; ++e) R[e] = 0.0;
       }
     }
   }

@@ -92,7 +92,8 @@ struct DevWork {
 // Device view of the problem data.  Tables hold i*P and i*Delta (real in the
 // real-phase kernel: T = double/float, complex otherwise).
 struct DevProblem {
-  int32_t S, n_tau, n_pairs, pad;
+  int32_t S, n_tau, n_pairs;
+  int32_t tc_stage;            // > 0: byte offset of the tensor-core staging area in dynamic shared memory (FP32 large blocks)
   double h, inv_h, beta;
   const int32_t *dims;
   const int32_t *ptab_off;     // [S] offset of sector s in the P table (elements)

@@ -74,14 +74,21 @@ cudaError_t launch_sobol_points(const uint32_t *m, const uint32_t *x0, int D, ui
 
 template <typename T, int ARENA, int RESMAX>
 static cudaError_t launch_t(const LaunchArgs &a) {
-  const size_t smem = eval_smem_bytes(a.threads, RESMAX, a.stage) + (size_t)a.extra_smem;
+  size_t smem = eval_smem_bytes(a.threads, RESMAX, a.stage) + (size_t)a.extra_smem;
+  DevProblem pb = a.pb;
+  pb.tc_stage = 0;
+  if (sizeof(T) == 4 && ARENA >= kArenaHuge && a.tc_omul) {   // per-warp staging after the other buffers
+    smem = (smem + 15) & ~(size_t)15;
+    pb.tc_stage = (int32_t)smem;
+    smem += (size_t)((a.threads + 31) / 32) * kTcWarpFloats * sizeof(float);
+  }
   auto *k = eval_kernel<T, ARENA, RESMAX, false>;
   cudaError_t e;
   if (smem > (48u << 10) && (e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
     return e;
   if (a.carveout >= 0 && (e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, a.carveout)))
     return e;
-  k<<<a.n_cta, a.threads, smem, a.stream>>>(a.pb, a.groups, a.works, a.cta_map, a.partials);
+  k<<<a.n_cta, a.threads, smem, a.stream>>>(pb, a.groups, a.works, a.cta_map, a.partials);
   return cudaGetLastError();
 }
 

@@ -36,6 +36,7 @@ struct LaunchArgs {
   bool extras;               // a work item has warped points or per-sample output
   bool stage;                // a group is scalar: shared-memory instruction staging buffers
   int extra_smem = 0;        // extra dynamic shared memory per CTA (occupancy tuning)
+  bool tc_omul = false;      // FP32: operator multiplies of 9-wide blocks on tensor cores (large-block kernels)
   int carveout = -1;         // preferred shared-memory carveout, percent (-1: driver default)
   cudaStream_t stream;
 };

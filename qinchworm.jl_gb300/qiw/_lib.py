@@ -28,6 +28,7 @@ QIW_GROUP_SIGMA = 3
 
 QIW_PREC_FP64 = 0
 QIW_PREC_FP32 = 1
+QIW_PREC_FP32_TC = 2
 QIW_TRANSFORM_DEFAULT = 0
 QIW_TRANSFORM_SORT = 1
 QIW_TRANSFORM_EXPMODEL = 2

@@ -219,6 +219,30 @@ def test_t2g_groups_match_oracle(device, kind, order, npa, N):
     assert _rel(got, want) < REL64
     got32 = device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32)[0]
     assert _rel(got32, want) < REL32
+    # operator multiplies of 9-wide blocks on tensor cores (3xTF32): the same FP32 bound
+    got_tc = device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32_TC)[0]
+    assert _rel(got_tc, want) < REL32
+
+
+@pytest.mark.parametrize("N", [16, 45])
+def test_t2g_tensor_core_operator_multiplies_match_fp32(device, N):
+    """QIW_PREC_FP32_TC against QIW_PREC_FP32 and the oracle on the heaviest t2g order-3 group,
+    with a sample count that leaves part of the last warp without a sample (those lanes run the
+    program for the warp's tensor-core multiplies and contribute nothing)."""
+    exp = models.t2g_bethe(n_tau=64)
+    g = exp.grid
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    tops = get_topologies_at_order(3, 3)
+    gid = device.create_group(_lib.QIW_GROUP_BOLD, 3, 3, tops)
+    t = (g.tau(0), g.tau(40), g.tau(41))
+    want = orc.OracleProblem(exp).integrate("bold", 3, 3, [(x.pairs, x.parity) for x in tops], *t, N)
+    got32 = device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32)[0]
+    got_tc = device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32_TC)[0]
+    rel_tc = _rel(got_tc, want)
+    print(f"t2g order 3 N={N}: FP32 {_rel(got32, want):.2e}, FP32 + tensor cores {rel_tc:.2e}")
+    assert rel_tc < REL32
+    assert _rel(got_tc, got32) < REL32
 
 
 @pytest.mark.parametrize("name,order", [("anderson", 1), ("anderson", 3), ("eg", 2)])
