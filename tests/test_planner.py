@@ -212,3 +212,63 @@ def test_reference_topology_eval_fixture():
     rel = np.abs(got - want).max(axis=1) / np.abs(want).max(axis=1)
     assert rel[distinct].max() < 2e-3
     assert np.median(rel) < 2e-3   # most samples agree even with shared cells
+
+
+def _reads(I):
+    """Arena ranges an instruction reads (start, length), as the kernel's interpreter does."""
+    op, r, k, c = int(I["op"]), int(I["rows"]), int(I["inner"]), int(I["cols"])
+    src, a, w = int(I["src"]), int(I["a"]), int(I["w"])
+    out = [(w, 1)] if w >= 0 else []
+    if op == 3:
+        out += [(a, r * r), (src, r * c)]
+    elif op == 5:
+        out += [(src, k * c)] + ([(int(I["dst"]), r * c)] if int(I["acc"]) else [])
+    elif op == 6:
+        out += [(src, r * c)] + ([(int(I["dst"]), r * c)] if int(I["acc"]) else [])
+    elif op == 7:
+        out += [(src, r * c)]
+    return out
+
+
+@pytest.mark.parametrize("model,order,npa", [("eg", 3, 2), ("eg", 4, 4), ("t2g", 2, 2), ("anderson", 3, 3)])
+def test_register_product_flags_are_consistent(model, order, npa):
+    """Planner flags for the FP32 interpreter's register-held products: an edge marked 'source
+    in registers' (bit 2) follows its node's P multiply marked 'keep' (bit 3) with no other
+    instruction in between, has that product's shape, and reads nothing of the arena copy; a
+    product marked 'no store' (bit 4) is read from the arena by no instruction before its slot
+    is written again.  Only blocks of dimension 1, 2, 4 are marked; 1x1 programs are not."""
+    exp = {"eg": lambda: models.eg_discrete_bath(n_tau=24), "t2g": lambda: models.t2g_bethe(n_tau=24),
+           "anderson": lambda: models.anderson(n_tau=24)}[model]()
+    pk = _lib.PackedProblem(exp)
+    tops = get_topologies_at_order(order, npa)
+    hp = pe.HostPlan(pk, _lib.QIW_GROUP_BOLD, order, npa, tops, arena_budget=20480 if model == "t2g" else 8192)
+    ins = hp.ins
+    flags = ins["flags"]
+    keep = None   # (index, rows, cols) of the last P multiply kept in registers
+    n_marked = 0
+    for i, I in enumerate(ins):
+        op, f = int(I["op"]), int(flags[i])
+        if op == 3 and f & 8:
+            keep = (i, int(I["rows"]), int(I["cols"]))
+            assert int(I["rows"]) in (1, 2, 4) and int(I["cols"]) in (1, 2, 4)
+            n_marked += 1
+            if f & 16:   # no instruction reads the product's slot before it is written again
+                lo, n = int(I["dst"]), int(I["rows"]) * int(I["cols"])
+                for J in ins[i + 1:]:
+                    fj = int(J["flags"])
+                    if not (int(J["op"]) in (5, 6) and fj & 4):
+                        assert all(s + m <= lo or s >= lo + n for s, m in _reads(J))
+                    if int(J["op"]) in (1, 2, 3, 4, 5, 6, 8, 9) and int(J["dst"]) < lo + n and \
+                            int(J["dst"]) + int(J["rows"]) * max(int(J["cols"]), 1) > lo and not int(J["acc"]):
+                        break
+            continue
+        if op in (5, 6) and f & 4:
+            assert keep is not None
+            assert int(I["inner" if op == 5 else "rows"]) == keep[1] and int(I["cols"]) == keep[2]
+            assert int(I["rows"]) in (1, 2, 4)
+            continue
+        keep = None
+    if model == "eg":
+        assert n_marked > 0
+    if model == "anderson":
+        assert n_marked == 0   # 1x1 programs fuse differently (PMAXPY)
