@@ -17,6 +17,7 @@ from typing import Optional
 
 import numpy as np
 
+from . import _lib
 from .device import Device, Work
 from .sobol import NumpyBitRNG, direction_numbers, scramble, sobol_points
 
@@ -43,39 +44,41 @@ class WarpFit:
     bias_sigma: float           # |mean difference| of the two estimators in standard errors
 
 
-def _replicas(dev: Device, work: Work, D: int, N: int, R: int, seed: int, warp_id):
-    out = []
+def _replicas(dev: Device, work: Work, D: int, N: int, R: int, seed: int, warp_id, precision):
+    """R scrambled replicas of the group's N-point estimate, all in one launch."""
+    wk = []
     for r in range(R):
         m, x0 = scramble(direction_numbers(D), NumpyBitRNG(seed + r))
-        wk = [Work(work.group, work.t_i, work.t_w, work.t_f, 0, N, N, m, x0)]
-        res = dev.integrate(wk, warps=None if warp_id is None else [warp_id])[0]
-        out.append(np.concatenate([b.ravel() for b in res]))
-    return np.array(out)
+        wk.append(Work(work.group, work.t_i, work.t_w, work.t_f, 0, N, N, m, x0))
+    res = dev.integrate(wk, precision, warps=None if warp_id is None else [warp_id] * R)
+    return np.array([np.concatenate([b.ravel() for b in blocks]) for blocks in res])
 
 
 def fit_group_warp(dev: Device, work: Work, n_train: int = 2 ** 15, steps: int = 600,
                    batch: int = 4096, lr: float = 3e-3, uniform_mix: float = 0.3,
                    N_test: int = 1024, R: int = 8, seed: int = 0,
-                   min_gain: float = 1.0) -> WarpFit:
+                   min_gain: float = 1.0, precision: int = _lib.QIW_PREC_FP32) -> WarpFit:
     """Train a warp for ``work``'s group at its inch times and decide whether to use it.
 
     Training data are ``n_train`` plain Sobol samples of the group (their per-sample values
     from qiw_integrate_samples, weight ||f||).  The decision compares the variances of R
-    scrambled replicas of N_test points each; the warp is kept when plain/warped > min_gain.
+    scrambled replicas of N_test points each (one launch per estimator); the warp is kept when
+    plain/warped > min_gain.  The fit's own integrand evaluations run in ``precision`` (FP32
+    chains by default: the fit needs |f| and variance ratios, not 1e-12 values).
     """
     order = dev.group_info[work.group][1]
     D = 2 * order
     if D < 2:
         return WarpFit(None, 1.0, 0.0, 0.0)
-    _, samples = dev.integrate_samples(Work(work.group, work.t_i, work.t_w, work.t_f, 0, n_train, n_train))
+    _, samples = dev.integrate_samples(Work(work.group, work.t_i, work.t_w, work.t_f, 0, n_train, n_train), precision)
     w = np.linalg.norm(samples, axis=1)
     if not np.any(w > 0):
         return WarpFit(None, 1.0, 0.0, 0.0)
     X = sobol_points(direction_numbers(D), 0, n_train)
     wid = dev.warp_create(D, seed=seed + 5, uniform_mix=uniform_mix)
     loss = dev.warp_train(wid, X, w + 1e-300, steps=steps, batch=batch, lr=lr)
-    plain = _replicas(dev, work, D, N_test, R, 1000 + seed, None)
-    warped = _replicas(dev, work, D, N_test, R, 1000 + seed, wid)
+    plain = _replicas(dev, work, D, N_test, R, 1000 + seed, None, precision)
+    warped = _replicas(dev, work, D, N_test, R, 1000 + seed, wid, precision)
     vp = float(np.sum(np.var(plain, axis=0, ddof=1)))
     vw = float(np.sum(np.var(warped, axis=0, ddof=1)))
     gain = vp / vw if vw > 0 else np.inf
