@@ -171,7 +171,10 @@ def _randomized(groups, sobol, launch, stat):
 class _Session:
     """Per-run state: device, problem upload and planned groups."""
 
-    def __init__(self, dev: Optional[Device], expansion):
+    def __init__(self, dev: Optional[Device], expansion, seq_offset: int = 0):
+        if seq_offset < 0:
+            raise ValueError("seq_offset must be non-negative")
+        self.seq_offset = int(seq_offset)   # leading Sobol points skipped by every sampled group
         self.dev = dev if dev is not None else Device(0)
         key = (id(expansion), len(expansion.corr_operators), len(expansion.pairs))
         if getattr(self.dev, "_expansion", None) is not expansion or getattr(self.dev, "_problem_key", None) != key:
@@ -217,6 +220,8 @@ class _Session:
             for i, seqs in items:
                 gid, td, D = entries[i]
                 start, length = (0, 1) if D == 0 else rank_sub_range(td.N_samples, comm)  # exact: once per rank
+                if D > 0:
+                    start += self.seq_offset
                 for m, x0 in seqs:
                     if m is not None and m.shape[0] > D:
                         m, x0 = np.ascontiguousarray(m[:D]), np.ascontiguousarray(x0[:D])
@@ -249,18 +254,22 @@ class _Session:
 
 
 def inchworm_step(expansion, t_i: float, t_w: float, t_f: float, top_data: Sequence[TopologiesInputData],
-                  dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm()):
-    """Regular inch step; returns (value, order_contribs, order_contribs_std) as SectorBlockMatrix."""
-    ses = _Session(dev, expansion)
+                  dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm(),
+                  seq_offset: int = 0):
+    """Regular inch step; returns (value, order_contribs, order_contribs_std) as SectorBlockMatrix.
+    seq_offset skips that many leading points of every sequence (skip!(seq, seq_offset,
+    exact=true) before the sum, src/scrambled_sobol.jl:189-208); 0 is the reference's run."""
+    ses = _Session(dev, expansion, seq_offset)
     ses.dev.set_ppgf(expansion.P)
     return _accumulate(ses.run(_lib.QIW_GROUP_BOLD, top_data, t_i, t_w, t_f, precision, comm), top_data,
                        expansion.dims)
 
 
 def inchworm_step_bare(expansion, t_i: float, t_f: float, top_data: Sequence[TopologiesInputData],
-                       dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm()):
-    """Initial step with bare propagators (all diagrams)."""
-    ses = _Session(dev, expansion)
+                       dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm(),
+                       seq_offset: int = 0):
+    """Initial step with bare propagators (all diagrams); seq_offset as in inchworm_step."""
+    ses = _Session(dev, expansion, seq_offset)
     return _accumulate(ses.run(_lib.QIW_GROUP_BARE, top_data, t_i, 0.0, t_f, precision, comm), top_data,
                        expansion.dims)
 
@@ -293,19 +302,23 @@ def _zero_P(expansion):
 def inchworm(expansion, orders, orders_bare, N_samples: int, n_pts_after_max: Optional[int] = None,
              rand_params: Optional[RandomizationParams] = None, dev: Optional[Device] = None,
              precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm(), n_steps: Optional[int] = None,
-             step_callback=None, warp_policy=None):
+             step_callback=None, warp_policy=None, seq_offset: int = 0):
     """inchworm!(expansion, grid, orders, orders_bare, N_samples; n_pts_after_max, rand_params).
 
     Writes the bold propagator into expansion.P and returns (P_orders, P_orders_std):
     dict order -> list of per-sector ImaginaryTimeGF.  `n_steps` stops after that many
     regular steps (the remaining grid points keep their atomic values).  `warp_policy`
     (qiw.warp.WarpPolicy) draws the samples of each bold group through a learned warp, refitted
-    every few steps and kept only where it lowers the variance; the estimates stay unbiased."""
+    every few steps and kept only where it lowers the variance; the estimates stay unbiased.
+    `seq_offset` > 0 skips that many leading points of every sequence (0: the reference's run).
+    With the unscrambled sequence its first point is the origin, where every integrated time
+    sits at the start of its segment; its single value can dominate the error of an N-point
+    estimate as an O(1/N) term, and seq_offset=1 leaves it out."""
     assert N_samples == 0 or (N_samples & (N_samples - 1)) == 0, "N_samples must be a power of 2"
     rp = rand_params or RandomizationParams()
     assert rp.N_seqs > 0
     grid = expansion.grid
-    ses = _Session(dev, expansion)
+    ses = _Session(dev, expansion, seq_offset)
     orders_all = sorted(set(orders) | set(orders_bare))
     P_orders = {o: _zero_P(expansion) for o in orders_all}
     P_orders_std = {o: _zero_P(expansion) for o in orders_all}
@@ -361,7 +374,8 @@ def inchworm(expansion, orders, orders_bare, N_samples: int, n_pts_after_max: Op
 
 
 def diff_inchworm(expansion, orders, N_samples: int, rand_params: Optional[RandomizationParams] = None,
-                  dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm()):
+                  dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm(),
+                  seq_offset: int = 0):
     """diff_inchworm!(expansion, grid, orders, N_samples; rand_params) (src/inchworm.jl:666-786).
 
     Differential inchworm: at every grid point tau_n the pseudo-particle self-energy
@@ -377,7 +391,7 @@ def diff_inchworm(expansion, orders, N_samples: int, rand_params: Optional[Rando
     rp = rand_params or RandomizationParams()
     assert rp.N_seqs > 0
     grid = expansion.grid
-    ses = _Session(dev, expansion)
+    ses = _Session(dev, expansion, seq_offset)
     top_data = []
     for o in orders:
         if o == 0:
@@ -421,6 +435,7 @@ def diff_inchworm(expansion, orders, N_samples: int, rand_params: Optional[Rando
 
 def correlator_2p(expansion, orders, N_samples: int, rand_params: Optional[RandomizationParams] = None,
                   dev: Optional[Device] = None, precision: int = _lib.QIW_PREC_FP64, comm: Comm = Comm(),
+                  seq_offset: int = 0,
                   request_std: bool = False, taus: Optional[Sequence[int]] = None):
     """correlator_2p(expansion, grid, orders, N_samples[, RequestStdDev()]).
 
@@ -431,7 +446,7 @@ def correlator_2p(expansion, orders, N_samples: int, rand_params: Optional[Rando
     assert N_samples == 0 or (N_samples & (N_samples - 1)) == 0, "N_samples must be a power of 2"
     rp = rand_params or RandomizationParams()
     grid = expansion.grid
-    ses = _Session(dev, expansion)
+    ses = _Session(dev, expansion, seq_offset)
     ses.dev.set_ppgf(expansion.P)
     top_data = []
     for o in orders:
@@ -494,6 +509,8 @@ def _run_multi_tau(ses: _Session, all_tds, spans, times, precision, comm, corrs)
             td = all_tds[ti]
             t_i, t_w, t_f = times[si]
             start, length = rank_sub_range(td.N_samples, comm) if D > 0 else (0, 1)
+            if D > 0:
+                start += ses.seq_offset
             for m, x0 in seqs:
                 works.append(Work(gid, t_i, t_w, t_f, start, length, td.N_samples, m, x0))
                 index.append(i)
