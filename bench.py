@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--n-max", type=int, default=2 ** 13, help="accuracy mode: largest swept N")
     ap.add_argument("--warp-n-max", type=int, default=0, help="accuracy mode: largest N of the warped FP32 arm (0: off)")
     ap.add_argument("--warp-refit", type=int, default=16, help="accuracy mode: refit the warps every this many steps")
+    ap.add_argument("--seq-offset", type=int, default=0,
+                    help="accuracy mode: skip this many leading Sobol points in every solve, the reference's too "
+                         "(1 leaves out the origin; the device-resident loop arms are then not run)")
     return ap.parse_args()
 
 
@@ -500,7 +503,7 @@ def run_ours(args):
     print(json.dumps(line))
 
 
-def _solve(model, n_tau, N, prec, dev, corr=False, device_loop=False, warp_policy=None):
+def _solve(model, n_tau, N, prec, dev, corr=False, device_loop=False, warp_policy=None, seq_offset=0):
     """Full inchworm! on the GPU; returns (P normalised by beta as arrays, G or None, seconds).
     device_loop: the whole loop on the device (qiw.batch, one CUDA graph) instead of the host
     loop with one launch per step.  Group plans come from the process's plan cache once a
@@ -520,12 +523,13 @@ def _solve(model, n_tau, N, prec, dev, corr=False, device_loop=False, warp_polic
         from qiw.batch import inchworm_batch
         inchworm_batch([exp], range(0, 5), range(0, 5), N, precision=prec, autotune=False)
     else:
-        inchworm(exp, range(0, 5), range(0, 5), N, dev=dev, precision=prec, warp_policy=warp_policy)
+        inchworm(exp, range(0, 5), range(0, 5), N, dev=dev, precision=prec, warp_policy=warp_policy,
+                 seq_offset=seq_offset)
     el = time.perf_counter() - t0
     ppgf.normalize_beta(exp.P, exp.grid.beta)
     G = None
     if corr:
-        G = np.array(correlator_2p(exp, range(0, 4), N, dev=dev, precision=prec))
+        G = np.array(correlator_2p(exp, range(0, 4), N, dev=dev, precision=prec, seq_offset=seq_offset))
     return [P_s.data.copy() for P_s in exp.P], G, el
 
 
@@ -542,17 +546,24 @@ def run_accuracy(args):
     dev = Device(int(os.environ.get("LOCAL_RANK", "0")))
     # one-time planning of every group (cold minus warm solve at N = 256); later solves reuse the plans
     dev.plan_cache_clear()
+    off = args.seq_offset
     t_cold = _solve(args.model, args.n_tau, 256, _lib.QIW_PREC_FP64, dev)[2]
     t_warm = _solve(args.model, args.n_tau, 256, _lib.QIW_PREC_FP64, dev)[2]
-    P_ref, _, t_ref = _solve(args.model, args.n_tau, args.n_ref, _lib.QIW_PREC_FP64, dev)
+    P_ref, _, t_ref = _solve(args.model, args.n_tau, args.n_ref, _lib.QIW_PREC_FP64, dev, seq_offset=off)
     sweep = []
     N = 256
     while N <= args.n_max:
         row = {"N": N}
-        P64, G64, t64 = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP64, dev, corr=(N == 1024))
-        P32, G32, t32 = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, corr=(N == 1024))
+        P64, G64, t64 = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP64, dev, corr=(N == 1024), seq_offset=off)
+        P32, G32, t32 = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, corr=(N == 1024), seq_offset=off)
         row.update(err_fp64=_perr(P64, P_ref), err_fp32=_perr(P32, P_ref), s_fp64=t64, s_fp32=t32,
                    fp32_vs_fp64_P=_perr(P32, P64))
+        if G64 is not None:
+            row["fp32_vs_fp64_G"] = float(np.abs(G32 - G64).max())
+        if off:   # the device-resident loop runs the reference's sequences only
+            sweep.append(row)
+            N *= 2
+            continue
         # the same solves with the loop on the device (warm: the first call pays the CUDA setup)
         if N == 256:
             _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, device_loop=True)
@@ -560,8 +571,6 @@ def run_accuracy(args):
         P32d, _, t32d = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, device_loop=True)
         row.update(err_fp64_dev=_perr(P64d, P_ref), err_fp32_dev=_perr(P32d, P_ref), s_fp64_dev=t64d,
                    s_fp32_dev=t32d, dev_vs_host_P=_perr(P64d, P64))
-        if G64 is not None:
-            row["fp32_vs_fp64_G"] = float(np.abs(G32 - G64).max())
         sweep.append(row)
         N *= 2
 
@@ -571,19 +580,19 @@ def run_accuracy(args):
         pol = WarpPolicy(refit_every=args.warp_refit, n_train=2 ** 14)
         N = 256
         while N <= args.warp_n_max:
-            Pw, _, tw = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, warp_policy=pol)
+            Pw, _, tw = _solve(args.model, args.n_tau, N, _lib.QIW_PREC_FP32, dev, warp_policy=pol, seq_offset=off)
             warped.append({"N": N, "err_warped_fp32": _perr(Pw, P_ref), "s_warped_fp32": tw})
             N *= 2
 
     def ttt(key_err, key_t):
         for r in sweep:
-            if r[key_err] <= 1e-4:
+            if key_err in r and r[key_err] <= 1e-4:
                 return r[key_t], r["N"]
         return None, None
 
     def first_below(rows, key_err, key_t, tol):
         for r in rows:
-            if r[key_err] <= tol:
+            if key_err in r and r[key_err] <= tol:
                 return r[key_t], r["N"]
         return None, None
 
@@ -598,7 +607,7 @@ def run_accuracy(args):
     t32d, n32d = ttt("err_fp32_dev", "s_fp32_dev")
     print(json.dumps({"mode": "accuracy", "metric": "time to 1e-4 max |P(tau) - P_ref(tau)|", "unit": "s",
                       "config": {"model": args.model, "n_tau": args.n_tau, "orders": "0:4", "N_ref": args.n_ref,
-                                 "reference": "plain FP64 GPU run at N_ref (Sobol, same grid)"},
+                                 "reference": "plain FP64 GPU run at N_ref (Sobol, same grid)", "seq_offset": off},
                       "time_to_1e-4_fp64": t64, "N_fp64": n64, "time_to_1e-4_fp32": t32, "N_fp32": n32,
                       "speedup_fp32": (t64 / t32) if (t64 and t32) else None,
                       "time_to_1e-4_fp64_device_loop": t64d, "N_fp64_device_loop": n64d,
