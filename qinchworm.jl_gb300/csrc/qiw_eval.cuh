@@ -56,6 +56,9 @@ constexpr int kRegTmp = 16;
 #ifndef QIW_BLOCK3
 #define QIW_BLOCK3 1
 #endif
+#ifndef QIW_PREFETCH_INSTR
+#define QIW_PREFETCH_INSTR 0
+#endif
 
 // Dynamic shared memory of the evaluation kernels: the reduction rows [warps][RESMAX] doubles,
 // then (launches with scalar programs) two instruction chunks of blockDim.x entries.
@@ -855,11 +858,22 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
       }
       cp_async_wait_0();
     } else if (active || tcx) {   // with tensor-core multiplies every lane runs the program
+#if QIW_PREFETCH_INSTR
+      // the next instruction's load is in flight while the current one executes
+      Instr nx = i0 < i1 ? load_instr(ins + i0) : Instr{};
+#pragma unroll 1
+      for (int ip = i0; ip < i1; ++ip) {
+        const Instr I = nx;
+        if (ip + 1 < i1) nx = load_instr(ins + ip + 1);
+        exec_instr<T, RESMAX, (ARENA >= kArenaHuge)>(I, A, O, R, tr, tcx);
+      }
+#else
 #pragma unroll 1
       for (int ip = i0; ip < i1; ++ip) {
         const Instr I = load_instr(ins + ip);
         exec_instr<T, RESMAX, (ARENA >= kArenaHuge)>(I, A, O, R, tr, tcx);
       }
+#endif
       if (!active) {   // a lane without a sample ran the program on an unset arena: no result
 #pragma unroll 1
         for (int e = 0; e < res_size; ++e) R[e] = 0.0;
