@@ -333,8 +333,12 @@ int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
   opt.arena_budget = kArenaLarge;
   if (const char *b = std::getenv("QIW_ARENA_BUDGET")) opt.arena_budget = std::max<int64_t>(256, std::atoll(b));
   opt.arena_budget = std::min<int64_t>(opt.arena_budget, kArenaLarge);
+  // tuning: split batches whose per-sample work exceeds this many flops (a thread runs a batch
+  // serially, so the heaviest batch bounds a launch's duration from below)
+  if (const char *m = std::getenv("QIW_MAX_BATCH_FLOPS")) opt.max_batch_flops = std::max(0.0, std::atof(m));
   std::string key = plan_key(c->hp, gs);
   key.append(reinterpret_cast<const char *>(&opt.arena_budget), sizeof(opt.arena_budget));
+  key.append(reinterpret_cast<const char *>(&opt.max_batch_flops), sizeof(opt.max_batch_flops));
   GroupRec *g = new GroupRec();
   if (std::shared_ptr<const Plan> hit = plan_store_find(key)) {
     g->plan = *hit;

@@ -34,6 +34,7 @@ struct PlanOptions {
   int64_t arena_budget = 4096;   // per-sample working-set budget (elements)
   bool fold_scalar_ops = true;   // fold 1x1 operator blocks into coefficients
   bool fuse_scalar = true;       // all sectors 1-dimensional: fuse a P multiply into its only AXPY
+  double max_batch_flops = 0.0;  // > 0: split batches above this many flops per sample (topology halves)
 };
 
 struct Plan {

@@ -1,5 +1,6 @@
 // Host-only access to the group planner (no CUDA): lets CPU tests execute a plan's
 // instruction stream against the CPU oracle.  Not part of the public ABI in include/qiw.h.
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -61,6 +62,7 @@ extern "C" int qiwp_batch_flops(const qiw_problem_desc *pd, const qiw_group_desc
   if (!rc) {
     PlanOptions opt;
     opt.arena_budget = arena_budget;
+    if (const char *m = std::getenv("QIW_MAX_BATCH_FLOPS")) opt.max_batch_flops = std::atof(m);
     rc = plan_group(hp, gs, opt, &p, &e);
   }
   if (rc) return -rc;
