@@ -57,7 +57,7 @@ constexpr int kRegTmp = 16;
 #define QIW_BLOCK3 1
 #endif
 #ifndef QIW_PREFETCH_INSTR
-#define QIW_PREFETCH_INSTR 0
+#define QIW_PREFETCH_INSTR 1
 #endif
 
 // Dynamic shared memory of the evaluation kernels: the reduction rows [warps][RESMAX] doubles,
@@ -859,7 +859,8 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
       cp_async_wait_0();
     } else if (active || tcx) {   // with tensor-core multiplies every lane runs the program
 #if QIW_PREFETCH_INSTR
-      // the next instruction's load is in flight while the current one executes
+      // the next instruction's load is in flight while the current one executes (FP32 eg step
+      // 15.4 -> 15.0 ms, t2g 149 -> 105 ms at 2048 samples, FP64 unchanged)
       Instr nx = i0 < i1 ? load_instr(ins + i0) : Instr{};
 #pragma unroll 1
       for (int ip = i0; ip < i1; ++ip) {
