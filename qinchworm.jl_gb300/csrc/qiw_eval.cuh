@@ -56,6 +56,9 @@ constexpr int kRegTmp = 16;
 #ifndef QIW_BLOCK3
 #define QIW_BLOCK3 1
 #endif
+#ifndef QIW_REG_PRODUCTS_FP64
+#define QIW_REG_PRODUCTS_FP64 0
+#endif
 #ifndef QIW_PREFETCH_INSTR
 #define QIW_PREFETCH_INSTR 1
 #endif
@@ -505,7 +508,7 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
 template <typename T, int RESMAX, bool LARGE>
 __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, double *R, T (&t)[kRegTmp],
                                            float *tcx) {
-  constexpr bool REG = QIW_REG_PRODUCTS && sizeof(T) == 4 && !LARGE;
+  constexpr bool REG = QIW_REG_PRODUCTS && (sizeof(T) == 4 || QIW_REG_PRODUCTS_FP64) && !LARGE;
   constexpr bool BLOCK3 = QIW_BLOCK3 && sizeof(T) == 4 && LARGE;
   const int rows = I.rows, cols = I.cols;
   switch (I.op) {
