@@ -59,9 +59,6 @@ constexpr int kRegTmp = 16;
 #ifndef QIW_REG_PRODUCTS_FP64
 #define QIW_REG_PRODUCTS_FP64 0
 #endif
-#ifndef QIW_NODE_EDGES
-#define QIW_NODE_EDGES 1
-#endif
 #ifndef QIW_PREFETCH_INSTR
 #define QIW_PREFETCH_INSTR 1
 #endif
@@ -503,43 +500,14 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
   }
 }
 
-// The register-source out-edges of a P multiply whose R x C product is in t[] (its
-// n_reg_edges following instructions): one loop that only tells OMUL from AXPY and the
-// target's row count apart, instead of a full instruction dispatch per edge.  The arithmetic
-// is omul_m / axpy_u with the source in registers, so results are unchanged.
-template <typename T, int R, int C>
-__device__ __forceinline__ void reg_edges(const Instr *__restrict__ e, int n, T *A, const T *O,
-                                          const T (&t)[kRegTmp]) {
-  Instr E = load_instr(e);
-#pragma unroll 1
-  for (int q = 0; q < n; ++q) {
-    const Instr I = E;
-    if (q + 1 < n) E = load_instr(e + q + 1);
-    const bool has_coef = (I.w >= 0) || has_c(I);
-    const T coef = edge_coef<T>(I, A);
-    const bool accf = I.acc != 0;
-    if (I.op == OP_OMUL) {
-      switch (I.rows) {
-        case 1: omul_ur<T, 1, R, C>(A, O, I.dst, I.a, I.src, coef, accf, has_coef, t); break;
-        case 2: omul_ur<T, 2, R, C>(A, O, I.dst, I.a, I.src, coef, accf, has_coef, t); break;
-        default: omul_ur<T, 4, R, C>(A, O, I.dst, I.a, I.src, coef, accf, has_coef, t); break;
-      }
-    } else {   // AXPY of the whole R x C product
-      axpy_u<T, R * C, true>(A, I.dst, I.src, coef, accf, has_coef, t);
-    }
-  }
-}
-
 // LARGE: the instantiation for problems with large sector blocks (the largest arena class, e.g.
 // t2g's 9 x 9 blocks), whose products take the 3-row register blocking; the others keep products
 // of dims 1, 2, 4 in registers.  Both only in the FP32 kernels: the FP64 kernels are DFMA-bound
 // and at the register budget of their launch bound, so they ignore flag bits 2-4 and keep
 // every product in the arena.  (One register budget cannot hold both paths without spills.)
-// Returns how many of the following instructions it consumed (a P multiply kept in registers
-// runs its register-source edges itself), 0 otherwise.
 template <typename T, int RESMAX, bool LARGE>
-__device__ __forceinline__ int exec_instr(const Instr &I, T *A, const T *O, double *R, T (&t)[kRegTmp],
-                                          float *tcx, const Instr *next) {
+__device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, double *R, T (&t)[kRegTmp],
+                                           float *tcx) {
   constexpr bool REG = QIW_REG_PRODUCTS && (sizeof(T) == 4 || QIW_REG_PRODUCTS_FP64) && !LARGE;
   constexpr bool BLOCK3 = QIW_BLOCK3 && sizeof(T) == 4 && LARGE;
   const int rows = I.rows, cols = I.cols;
@@ -580,11 +548,6 @@ __device__ __forceinline__ int exec_instr(const Instr &I, T *A, const T *O, doub
         const int code = cr * 3 + cc;
         const bool store = (I.flags & 16u) == 0;
         QIW_D2(pmul_r, A, t, I.dst, I.a, I.src, store)
-        if (QIW_NODE_EDGES && I.n_reg_edges) {
-          const int n = I.n_reg_edges;
-          QIW_D2(reg_edges, next, n, A, O, t)
-          return n;
-        }
       } else if (cr >= 0 && cc >= 0) {
         const int code = cr * 3 + cc;
         QIW_D2(pmul_u, A, I.dst, I.a, I.src)
@@ -683,7 +646,6 @@ __device__ __forceinline__ int exec_instr(const Instr &I, T *A, const T *O, doub
     default:
       break;
   }
-  return 0;
 }
 
 // Times and sample range of one tile: t_i, t_w, t_f of the work item, the Sobol index of its
@@ -717,6 +679,7 @@ __device__ __forceinline__ void sample_setup(const DevProblem &pb, const DevGrou
       const uint64_t n = w.first_index + sidx;
       const uint32_t gray = (uint32_t)(n ^ (n >> 1));
       double u[kMaxDim];
+#pragma unroll 1
       if (EXTRAS && w.pts) {  // warped point x = w(y) of a learned change of variables, weight 1/q(x)
         const double *pp = w.pts + sidx * (uint64_t)(D + 1);
 #pragma unroll 1
@@ -906,17 +869,13 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
       for (int ip = i0; ip < i1; ++ip) {
         const Instr I = nx;
         if (ip + 1 < i1) nx = load_instr(ins + ip + 1);
-        const int used = exec_instr<T, RESMAX, (ARENA >= kArenaHuge)>(I, A, O, R, tr, tcx, ins + ip + 1);
-        if (used) {
-          ip += used;
-          if (ip + 1 < i1) nx = load_instr(ins + ip + 1);
-        }
+        exec_instr<T, RESMAX, (ARENA >= kArenaHuge)>(I, A, O, R, tr, tcx);
       }
 #else
 #pragma unroll 1
       for (int ip = i0; ip < i1; ++ip) {
         const Instr I = load_instr(ins + ip);
-        ip += exec_instr<T, RESMAX, (ARENA >= kArenaHuge)>(I, A, O, R, tr, tcx, ins + ip + 1);
+        exec_instr<T, RESMAX, (ARENA >= kArenaHuge)>(I, A, O, R, tr, tcx);
       }
 #endif
       if (!active) {   // a lane without a sample ran the program on an unset arena: no result

@@ -27,8 +27,7 @@ struct alignas(16) Instr {     // 32 bytes
   uint8_t op, rows, inner, cols;
   uint8_t acc;                 // 1: accumulate into dst, 0: overwrite
   uint8_t flags;               // bit 0: c != 1, bit 1: c == -1 (set on upload; the kernels test no doubles)
-  uint8_t n_reg_edges;         // P multiply kept in registers: this many following instructions are its register-source edges
-  uint8_t pad2;
+  uint8_t pad1, pad2;
   int32_t dst;                 // arena offset (elements)
   int32_t src;                 // arena offset (elements)
   int32_t a;                   // Pm offset (arena) / operator value offset / result offset

@@ -504,9 +504,6 @@ struct Builder {
       if (pmul_at >= 0) {   // the out-edges above read the product from registers
         ins[pmul_at].flags |= kFlagKeepReg;
         if (!tmp_read) ins[pmul_at].flags |= kFlagNoStore;
-        int n = 0;   // the run of register-source edges right after the multiply (<= 255)
-        for (size_t q = (size_t)pmul_at + 1; q < ins.size() && n < 255 && (ins[q].flags & kFlagSrcReg); ++q) ++n;
-        ins[pmul_at].n_reg_edges = (uint8_t)n;
       }
       if (!tmp_taken) al.release(tmp, (int64_t)d * d0);
       for (auto it = ready.rbegin(); it != ready.rend(); ++it) stack.push_back(*it);

@@ -15,7 +15,7 @@ from qiw import _lib, build as qbuild
 from qiw.sobol import ScrambledSobolSeq
 
 INSTR = np.dtype([("op", "u1"), ("rows", "u1"), ("inner", "u1"), ("cols", "u1"), ("acc", "u1"),
-                  ("flags", "u1"), ("n_reg_edges", "u1"), ("pad", "u1"), ("dst", "<i4"), ("src", "<i4"), ("a", "<i4"), ("w", "<i4"), ("c", "<f8")])
+                  ("flags", "u1"), ("pad", "u1", 2), ("dst", "<i4"), ("src", "<i4"), ("a", "<i4"), ("w", "<i4"), ("c", "<f8")])
 PMJOB = np.dtype([("iv", "<i2"), ("s", "<i2"), ("off", "<i4")])
 WJOB = np.dtype([("head", "<i2"), ("tail", "<i2"), ("pair", "<i2"), ("pad", "<i2"), ("off", "<i4")])
 
