@@ -679,7 +679,6 @@ __device__ __forceinline__ void sample_setup(const DevProblem &pb, const DevGrou
       const uint64_t n = w.first_index + sidx;
       const uint32_t gray = (uint32_t)(n ^ (n >> 1));
       double u[kMaxDim];
-#pragma unroll 1
       if (EXTRAS && w.pts) {  // warped point x = w(y) of a learned change of variables, weight 1/q(x)
         const double *pp = w.pts + sidx * (uint64_t)(D + 1);
 #pragma unroll 1
