@@ -363,10 +363,11 @@ def run_reference(args):
 
 
 # DRAM bytes (read + write) of one eval_kernel launch of the default FP64 eg inch step, from one
-# ncu capture of `python bench.py --steps 2 --warmup 1 --no-cpu-baseline` (dram__bytes_read.sum
-# 22.63 GB + dram__bytes_write.sum 27.35 GB at 1024 samples, one pass): the per-thread arenas
-# spilling from L2.  It grows with the samples; other workloads report null.
-EG_FP64_TRAFFIC_PER_1024 = 49.98e9
+# ncu capture of `python bench.py --steps 2 --warmup 3 --no-cpu-baseline --no-parity
+# --no-time-to-tol` (dram__bytes_read.sum 22.80 GB + dram__bytes_write.sum 27.60 GB at 1024
+# samples, one pass): the per-thread arenas spilling from L2.  It grows with the samples; other
+# workloads report null.
+EG_FP64_TRAFFIC_PER_1024 = 50.40e9
 
 
 def _traffic(args):
