@@ -142,7 +142,7 @@ int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
   t->cta_first.assign(n_work, 0);
   t->res_sizes.assign(n_work, 0);
   t->out_off.assign(n_work, 0);
-  const int threads = c->threads;  // samples per tile
+  const int threads = precision == QIW_PREC_FP64 ? c->threads : c->threads32;  // samples per tile
   for (int i = 0; i < n_work; ++i) {
     const qiw_work_desc &wd = work[i];
     if (wd.group < 0 || wd.group >= (int)c->groups.size()) return c->fail(QIW_ERR_ARG, "qiw_integrate: bad group id");
@@ -252,7 +252,7 @@ int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const De
   la.cta_map = cta_map;
   la.partials = partials;
   la.n_cta = n_cta;
-  la.threads = c->threads;
+  la.threads = precision == QIW_PREC_FP64 ? c->threads : c->threads32;
   la.extra_smem = c->eval_extra_smem;
   la.carveout = c->eval_carveout;
   la.arena_max = t.arena_max;
@@ -436,7 +436,7 @@ int qiw_ctx_create(qiw_ctx **out, int device) {
   }
   if (const char *t = std::getenv("QIW_THREADS")) {
     int v = std::atoi(t);
-    if (v == 32 || v == 64 || v == 96 || v == 128) c->threads = v;
+    if (v == 32 || v == 64 || v == 96 || v == 128) c->threads = c->threads32 = v;
   }
   if (const char *t = std::getenv("QIW_EVAL_EXTRA_SMEM")) c->eval_extra_smem = std::max(0, std::min(160 << 10, std::atoi(t)));
   if (const char *t = std::getenv("QIW_EVAL_CARVEOUT")) c->eval_carveout = std::max(-1, std::min(100, std::atoi(t)));

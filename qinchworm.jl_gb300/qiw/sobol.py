@@ -88,16 +88,12 @@ def scramble(m: np.ndarray, rng) -> tuple[np.ndarray, np.ndarray]:
     for d in range(D):
         ltm[d] = np.tril(ltm[d])
         np.fill_diagonal(ltm[d], 1)
-    out = m.astype(np.uint64).copy()
-    for d in range(D):
-        rows = [sum(int(ltm[d, p, k]) << (31 - k) for k in range(32)) for p in range(32)]
-        for j in range(32):
-            mdj = int(m[d, j])
-            t2 = 0
-            for p in range(31, -1, -1):
-                t1 = bin(rows[p] & mdj).count("1") & 1
-                t2 |= t1 << (31 - p)
-            out[d, j] = t2
+    # bit p of the scrambled m[d, j] (from the top: 31 - p) is the GF(2) dot product of row p of
+    # the lower-triangular matrix with the bits of m[d, j] (k-th bit from the top, 31 - k)
+    shifts = (31 - np.arange(32)).astype(np.uint64)
+    mbits = ((m.astype(np.uint64)[:, None, :] >> shifts[None, :, None]) & np.uint64(1)).astype(np.int64)  # [D][k][j]
+    prod = np.einsum("dpk,dkj->dpj", ltm.astype(np.int64), mbits) & 1                                     # [D][p][j]
+    out = (prod.astype(np.uint64) << shifts[None, :, None]).sum(axis=1, dtype=np.uint64)                   # [D][j]
     return out.astype(np.uint32), (x0 & 0xFFFFFFFF).astype(np.uint32)
 
 

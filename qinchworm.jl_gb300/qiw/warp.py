@@ -44,12 +44,10 @@ class WarpFit:
     bias_sigma: float           # |mean difference| of the two estimators in standard errors
 
 
-def _replicas(dev: Device, work: Work, D: int, N: int, R: int, seed: int, warp_id, precision):
-    """R scrambled replicas of the group's N-point estimate, all in one launch."""
-    wk = []
-    for r in range(R):
-        m, x0 = scramble(direction_numbers(D), NumpyBitRNG(seed + r))
-        wk.append(Work(work.group, work.t_i, work.t_w, work.t_f, 0, N, N, m, x0))
+def _replicas(dev: Device, work: Work, seqs, N: int, warp_id, precision):
+    """The group's N-point estimate on each scrambled sequence (m, x0) of seqs, in one launch."""
+    R = len(seqs)
+    wk = [Work(work.group, work.t_i, work.t_w, work.t_f, 0, N, N, m, x0) for (m, x0) in seqs]
     res = dev.integrate(wk, precision, warps=None if warp_id is None else [warp_id] * R)
     return np.array([np.concatenate([b.ravel() for b in blocks]) for blocks in res])
 
@@ -77,8 +75,9 @@ def fit_group_warp(dev: Device, work: Work, n_train: int = 2 ** 15, steps: int =
     X = sobol_points(direction_numbers(D), 0, n_train)
     wid = dev.warp_create(D, seed=seed + 5, uniform_mix=uniform_mix)
     loss = dev.warp_train(wid, X, w + 1e-300, steps=steps, batch=batch, lr=lr)
-    plain = _replicas(dev, work, D, N_test, R, 1000 + seed, None, precision)
-    warped = _replicas(dev, work, D, N_test, R, 1000 + seed, wid, precision)
+    seqs = [scramble(direction_numbers(D), NumpyBitRNG(1000 + seed + r)) for r in range(R)]
+    plain = _replicas(dev, work, seqs, N_test, None, precision)
+    warped = _replicas(dev, work, seqs, N_test, wid, precision)
     vp = float(np.sum(np.var(plain, axis=0, ddof=1)))
     vw = float(np.sum(np.var(warped, axis=0, ddof=1)))
     gain = vp / vw if vw > 0 else np.inf
