@@ -248,10 +248,8 @@ def time_to_tol(dev, step=200, n_loop=256, tols=(1e-3, 1e-4), n_ref=2 ** 20, n_m
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     wmap, kept = {}, 0
-    for (o, gid) in gids:
-        if o == 0:
-            continue
-        fit = qwarp.fit_group_warp(dev, Work(gid, *t, 0, 0, 0))
+    fitted = [gid for (o, gid) in gids if o > 0]
+    for gid, fit in zip(fitted, qwarp.fit_group_warps(dev, [Work(gid, *t, 0, 0, 0) for gid in fitted])):
         wmap[gid] = -1 if fit.warp_id is None else fit.warp_id
         kept += fit.warp_id is not None
     torch.cuda.synchronize()

@@ -190,6 +190,12 @@ int qiw_warp_grad(qiw_ctx *ctx, int32_t warp_id, const double *x, const double *
 /* Adam on minibatches of (x_i in [0,1)^D, w_i = |f(x_i)|) produced by plain qMC. */
 int qiw_warp_train(qiw_ctx *ctx, int32_t warp_id, const double *x, const double *w, int64_t n, int32_t steps,
                    int32_t batch, double lr, double *final_loss);
+/* qiw_warp_train of n_warps distinct warps at once (warp k on x[k] [n[k]][D_k], w[k] [n[k]]),
+ * trained concurrently on the device; final_loss (optional) receives n_warps values.  The
+ * results equal n_warps qiw_warp_train calls. */
+int qiw_warp_train_batch(qiw_ctx *ctx, int32_t n_warps, const int32_t *warp_ids, const double *const *x,
+                         const double *const *w, const int64_t *n, int32_t steps, int32_t batch, double lr,
+                         double *final_loss);
 /* Warped points of Sobol indices first..first+n-1: [n][D + 1] = (x_1..x_D, 1/q(x)). */
 int qiw_warp_map(qiw_ctx *ctx, int32_t warp_id, const uint32_t *sobol_m, const uint32_t *sobol_x0,
                  uint64_t first, uint64_t n, double *points);
@@ -200,6 +206,10 @@ int qiw_integrate_warped(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work
  * samples[n_samples][sum d_s^2] (real parts f_i with out = -i * J / N * sum_i f_i). */
 int qiw_integrate_samples(qiw_ctx *ctx, const qiw_work_desc *work, int32_t precision, double *out,
                           double *samples);
+/* The same for n_work work items in one launch: out as qiw_integrate, samples holds the items'
+ * per-sample values one after another (item i: [n_samples_i][sum d_s^2]). */
+int qiw_integrate_samples_batch(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, int32_t precision,
+                                double *out, double *samples);
 
 /* Kernel time of the most recent qiw_integrate (ms, CUDA events on the context stream). */
 double qiw_last_kernel_ms(const qiw_ctx *ctx);

@@ -95,12 +95,18 @@ int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
       }
     }
   }
+  // per-sample values: one region per work item, in work order
+  size_t n_sample_vals = 0;
   if (sample_out) {
-    const size_t n = (size_t)t.works[0].n_samples * t.res_sizes[0];
-    if ((rc = c->cuda(c->d_samples.reserve(n), "alloc samples")) ||
-        (rc = c->cuda(cudaMemsetAsync(c->d_samples.p, 0, sizeof(double) * n, st), "clear samples")))
+    for (int i = 0; i < n_work; ++i) n_sample_vals += (size_t)t.works[i].n_samples * t.res_sizes[i];
+    if ((rc = c->cuda(c->d_samples.reserve(n_sample_vals), "alloc samples")) ||
+        (rc = c->cuda(cudaMemsetAsync(c->d_samples.p, 0, sizeof(double) * n_sample_vals, st), "clear samples")))
       return rc;
-    t.works[0].sample_out = c->d_samples.p;
+    size_t o = 0;
+    for (int i = 0; i < n_work; ++i) {
+      t.works[i].sample_out = c->d_samples.p + o;
+      o += (size_t)t.works[i].n_samples * t.res_sizes[i];
+    }
   }
   const int n_cta = (int)t.cta_map.size();
   int zero = 0;
@@ -120,9 +126,8 @@ int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
   if ((rc = c->cuda(cudaMemcpyAsync(out, c->d_out.p, sizeof(double) * 2 * t.out_total, cudaMemcpyDeviceToHost, st), "copy out")) ||
       (rc = c->cuda(cudaMemcpyAsync(&err_word, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "copy err")))
     return rc;
-  if (sample_out &&
-      (rc = c->cuda(cudaMemcpyAsync(sample_out, c->d_samples.p,
-                                    sizeof(double) * (size_t)t.works[0].n_samples * t.res_sizes[0],
+  if (sample_out && n_sample_vals > 0 &&
+      (rc = c->cuda(cudaMemcpyAsync(sample_out, c->d_samples.p, sizeof(double) * n_sample_vals,
                                     cudaMemcpyDeviceToHost, st), "copy samples")))
     return rc;
   if ((rc = c->cuda(cudaStreamSynchronize(st), "integrate"))) return rc;
@@ -448,6 +453,7 @@ void qiw_ctx_destroy(qiw_ctx *c) {
   if (!c) return;
   qiw::DeviceScope dev_scope(c->device);
   cudaStreamSynchronize(c->stream);
+  for (cudaStream_t s : c->aux) cudaStreamSynchronize(s);
   c->clear_groups();
   destroy_warps(c);
   c->d_groups.release();
@@ -461,6 +467,8 @@ void qiw_ctx_destroy(qiw_ctx *c) {
   c->d_works.release();
   c->d_cta_map.release();
   c->d_sobol.release();
+  for (cudaStream_t s : c->aux) cudaStreamDestroy(s);
+  for (cudaEvent_t e : c->aux_ev) cudaEventDestroy(e);
   cudaEventDestroy(c->ev0);
   cudaEventDestroy(c->ev1);
   cudaStreamDestroy(c->stream);
@@ -640,6 +648,12 @@ int qiw_integrate_warped(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, 
 int qiw_integrate_samples(qiw_ctx *c, const qiw_work_desc *work, int32_t precision, double *out, double *samples) {
   if (!c || !work || !samples) return QIW_ERR_ARG;
   return integrate_impl(c, 1, work, precision, out, nullptr, samples);
+}
+
+int qiw_integrate_samples_batch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision,
+                                double *out, double *samples) {
+  if (!c || n_work < 0 || (n_work > 0 && (!work || !out || !samples))) return QIW_ERR_ARG;
+  return integrate_impl(c, n_work, work, precision, out, nullptr, samples);
 }
 
 int qiw_sobol_points(qiw_ctx *c, int32_t D, const uint32_t *m, const uint32_t *x0, uint64_t first, uint64_t n,

@@ -67,6 +67,7 @@ struct GroupRec {
 };
 
 struct WarpRec;
+constexpr int kAuxStreams = 16;   // most warps trained concurrently, one stream each
 
 // Host-side launch tables of one qiw_integrate call.
 struct LaunchTables {
@@ -113,6 +114,8 @@ struct qiw_ctx {
   qiw::DevBuf<uint32_t> d_sobol;
   qiw::DevBuf<double> d_pts, d_samples;
   std::vector<qiw::WarpRec *> warps;
+  std::vector<cudaStream_t> aux;   // streams of concurrent warp training (created on first use)
+  std::vector<cudaEvent_t> aux_ev; // their fork / join events
   int threads = 64;            // samples per tile of the FP64 launches
   int threads32 = 128;         // samples per tile of the FP32 launches (eg step 15.2 -> 14.6 ms against 64)
   int eval_extra_smem = 0;     // tuning: extra dynamic shared memory per CTA (limits CTAs per SM)

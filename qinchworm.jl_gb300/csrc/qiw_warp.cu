@@ -686,7 +686,7 @@ static int upload_batch(qiw_ctx *c, WarpRec *w, const double *x, const double *w
 
 // Gradient and loss of n samples into w->g and w->loss: one made_grad_tc_kernel block per 64
 // samples writes its own row, grad_reduce_kernel sums the rows in block order.
-static int run_grad(qiw_ctx *c, WarpRec *w, const float *X, const float *wt, int64_t n) {
+static int run_grad(qiw_ctx *c, WarpRec *w, const float *X, const float *wt, int64_t n, cudaStream_t st) {
   const int Lw = Layout(w->D).n;
   const unsigned blocks = (unsigned)((n + WTILE - 1) / WTILE);
   int rc;
@@ -699,14 +699,13 @@ static int run_grad(qiw_ctx *c, WarpRec *w, const float *X, const float *wt, int
     const size_t smem = tc_grad_smem<DD>();                                                                  \
     e = cudaFuncSetAttribute(made_grad_tc_kernel<DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
     if (e == cudaSuccess)                                                                                    \
-      made_grad_tc_kernel<DD><<<blocks, 128, smem, c->stream>>>(w->wq.p, w->alpha, X, wt, (int)n, w->gpart.p, w->lpart.p); \
+      made_grad_tc_kernel<DD><<<blocks, 128, smem, st>>>(w->wq.p, w->alpha, X, wt, (int)n, w->gpart.p, w->lpart.p); \
   }
   QIW_WARP_D_SWITCH(w->D, QIW_GRAD_CALL)
 #undef QIW_GRAD_CALL
   if (e != cudaSuccess) return c->cuda(e, "warp grad kernel: shared memory");
   if ((rc = c->cuda(cudaGetLastError(), "warp grad kernel"))) return rc;
-  grad_reduce_kernel<<<(Lw + 255) / 256, 256, 0, c->stream>>>(w->gpart.p, w->lpart.p, (int)blocks, Lw, w->g.p,
-                                                              w->loss.p);
+  grad_reduce_kernel<<<(Lw + 255) / 256, 256, 0, st>>>(w->gpart.p, w->lpart.p, (int)blocks, Lw, w->g.p, w->loss.p);
   return c->cuda(cudaGetLastError(), "warp grad reduce kernel");
 }
 
@@ -717,7 +716,7 @@ int qiw_warp_grad(qiw_ctx *c, int32_t id, const double *x, const double *wt, int
   if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_warp_grad: cudaSetDevice");
   WarpRec *w = c->warps[id];
   int rc = upload_batch(c, w, x, wt, n);
-  if (rc || (rc = run_grad(c, w, w->X.p, w->w.p, n))) return rc;
+  if (rc || (rc = run_grad(c, w, w->X.p, w->w.p, n, c->stream))) return rc;
   const int Lw = Layout(w->D).n;
   std::vector<float> g(Lw);
   float loss = 0.f;
@@ -734,34 +733,88 @@ int qiw_warp_train(qiw_ctx *c, int32_t id, const double *x, const double *wt, in
                    int32_t batch, double lr, double *final_loss) {
   if (!c || !x || !wt || id < 0 || id >= (int)c->warps.size() || n <= 0 || steps < 0 || batch <= 0)
     return QIW_ERR_ARG;
-  qiw::DeviceScope dev_scope(c->device);
-  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_warp_fit: cudaSetDevice");
-  WarpRec *w = c->warps[id];
-  // whole-set normalisation; minibatch b covers samples [b*batch, (b+1)*batch) cyclically
-  int rc = upload_batch(c, w, x, wt, n);
-  if (rc) return rc;
-  const int Lw = Layout(w->D).n;
-  const int64_t nb = std::max<int64_t>(1, n / batch);
-  float loss = 0.f;
-  for (int s = 0; s < steps; ++s) {
-    const int64_t b = s % nb;
-    const int64_t lo = b * batch, cnt = std::min<int64_t>(batch, n - lo);
-    if ((rc = run_grad(c, w, w->X.p + lo * w->D, w->w.p + lo, cnt))) return rc;
-    w->t += 1;
-    const float b1 = 0.9f, b2 = 0.999f;
-    const float c1 = 1.f - std::pow(b1, (float)w->t), c2 = 1.f - std::pow(b2, (float)w->t);
-    // the minibatch gradient is scaled by n/cnt so its size does not depend on the batch
-    const float scale_lr = (float)lr;
-    adam_kernel<<<64, 256, 0, c->stream>>>(w->p.p, w->m.p, w->v.p, w->g.p, w->mask.p, w->wq.p, Lw, scale_lr, b1, b2,
-                                           1e-8f, c1, c2);
-    if ((rc = c->cuda(cudaGetLastError(), "adam kernel"))) return rc;
+  return qiw_warp_train_batch(c, 1, &id, &x, &wt, &n, steps, batch, lr, final_loss);
+}
+
+int qiw_warp_train_batch(qiw_ctx *c, int32_t n_warps, const int32_t *ids, const double *const *x,
+                         const double *const *wt, const int64_t *n, int32_t steps, int32_t batch, double lr,
+                         double *final_loss) {
+  if (!c || n_warps < 0 || (n_warps > 0 && (!ids || !x || !wt || !n)) || steps < 0 || batch <= 0) return QIW_ERR_ARG;
+  for (int k = 0; k < n_warps; ++k) {
+    if (ids[k] < 0 || ids[k] >= (int)c->warps.size() || !x[k] || !wt[k] || n[k] <= 0) return QIW_ERR_ARG;
+    for (int j = 0; j < k; ++j)
+      if (ids[j] == ids[k]) return c->fail(QIW_ERR_ARG, "qiw_warp_train_batch: a warp appears twice");
   }
-  if (final_loss) {
-    if ((rc = run_grad(c, w, w->X.p, w->w.p, n)) ||
-        (rc = c->cuda(cudaMemcpyAsync(&loss, w->loss.p, sizeof(float), cudaMemcpyDeviceToHost, c->stream), "warp")) ||
-        (rc = c->cuda(cudaStreamSynchronize(c->stream), "warp")))
+  if (n_warps == 0) return QIW_OK;
+  qiw::DeviceScope dev_scope(c->device);
+  if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_warp_train: cudaSetDevice");
+  // Uploads (whole-set normalisation) and every buffer a step uses, reserved before any step
+  // runs: minibatch b of warp k covers its samples [b*batch, (b+1)*batch) cyclically.
+  int rc;
+  for (int k = 0; k < n_warps; ++k) {
+    WarpRec *w = c->warps[ids[k]];
+    const size_t blocks = (size_t)((n[k] + WTILE - 1) / WTILE);
+    if ((rc = upload_batch(c, w, x[k], wt[k], n[k])) ||
+        (rc = c->cuda(w->gpart.reserve(blocks * Layout(w->D).n), "warp grad partials")) ||
+        (rc = c->cuda(w->lpart.reserve(blocks), "warp grad partials")))
       return rc;
-    *final_loss = loss;
+  }
+  // One warp trains on the context stream; several train concurrently, warp k on auxiliary
+  // stream k mod kAuxStreams (its steps stay in order there), forked from and joined back into
+  // the context stream.  Each warp owns its parameters, moments and gradient rows, so the
+  // results are those of training the warps one after another.
+  const int n_st = n_warps == 1 ? 0 : std::min(n_warps, kAuxStreams);
+  for (int i = (int)c->aux.size(); i < n_st; ++i) {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev = nullptr;
+    if ((rc = c->cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "warp train: streams"))) return rc;
+    if ((rc = c->cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "warp train: streams"))) {
+      cudaStreamDestroy(s);
+      return rc;
+    }
+    c->aux.push_back(s);
+    c->aux_ev.push_back(ev);
+  }
+  if (n_st > 0) {
+    if ((rc = c->cuda(cudaEventRecord(c->aux_ev[0], c->stream), "warp train: fork"))) return rc;
+    for (int i = 0; i < n_st; ++i)
+      if ((rc = c->cuda(cudaStreamWaitEvent(c->aux[i], c->aux_ev[0], 0), "warp train: fork"))) return rc;
+  }
+  auto stream_of = [&](int k) { return n_st == 0 ? c->stream : c->aux[k % n_st]; };
+  const float b1 = 0.9f, b2 = 0.999f;
+  for (int s = 0; s < steps; ++s) {
+    for (int k = 0; k < n_warps; ++k) {
+      WarpRec *w = c->warps[ids[k]];
+      cudaStream_t st = stream_of(k);
+      const int64_t nb = std::max<int64_t>(1, n[k] / batch);
+      const int64_t lo = (s % nb) * batch, cnt = std::min<int64_t>(batch, n[k] - lo);
+      if ((rc = run_grad(c, w, w->X.p + lo * w->D, w->w.p + lo, cnt, st))) return rc;
+      w->t += 1;
+      const float c1 = 1.f - std::pow(b1, (float)w->t), c2 = 1.f - std::pow(b2, (float)w->t);
+      adam_kernel<<<64, 256, 0, st>>>(w->p.p, w->m.p, w->v.p, w->g.p, w->mask.p, w->wq.p, Layout(w->D).n, (float)lr,
+                                      b1, b2, 1e-8f, c1, c2);
+      if ((rc = c->cuda(cudaGetLastError(), "adam kernel"))) return rc;
+    }
+  }
+  if (final_loss)
+    for (int k = 0; k < n_warps; ++k) {
+      WarpRec *w = c->warps[ids[k]];
+      if ((rc = run_grad(c, w, w->X.p, w->w.p, n[k], stream_of(k)))) return rc;
+    }
+  if (n_st > 0)
+    for (int i = 0; i < n_st; ++i)
+      if ((rc = c->cuda(cudaEventRecord(c->aux_ev[i], c->aux[i]), "warp train: join")) ||
+          (rc = c->cuda(cudaStreamWaitEvent(c->stream, c->aux_ev[i], 0), "warp train: join")))
+        return rc;
+  if (final_loss) {
+    std::vector<float> loss(n_warps, 0.f);
+    for (int k = 0; k < n_warps; ++k)
+      if ((rc = c->cuda(cudaMemcpyAsync(&loss[k], c->warps[ids[k]]->loss.p, sizeof(float), cudaMemcpyDeviceToHost,
+                                        c->stream), "warp")))
+        return rc;
+    if ((rc = c->cuda(cudaStreamSynchronize(c->stream), "warp train"))) return rc;
+    for (int k = 0; k < n_warps; ++k) final_loss[k] = loss[k];
+    return QIW_OK;
   }
   return c->cuda(cudaStreamSynchronize(c->stream), "warp train");
 }

@@ -158,6 +158,18 @@ class Device:
         self._check(self.lib.qiw_integrate_samples(self.h, descs, precision, out.ctypes.data, samples.ctypes.data))
         return self._unpack(out, 1)[0], samples
 
+    def integrate_samples_batch(self, works: Sequence[Work], precision: int = _lib.QIW_PREC_FP64):
+        """integrate_samples of several work items in one launch: (blocks per item, per-sample
+        values per item [n_samples_i][sum d^2])."""
+        descs, keep = self._descs(works)
+        rs = int(np.sum(self.packed.dims ** 2))
+        out = np.zeros(2 * rs * len(works))
+        samples = np.zeros((sum(w.n_samples for w in works), rs))
+        self._check(self.lib.qiw_integrate_samples_batch(self.h, len(works), descs, precision, out.ctypes.data,
+                                                         samples.ctypes.data))
+        cut = np.cumsum([0] + [w.n_samples for w in works])
+        return self._unpack(out, len(works)), [samples[a:b] for a, b in zip(cut[:-1], cut[1:])]
+
     # -- learned warps --------------------------------------------------------------
     def warp_create(self, D: int, seed: int = 0, uniform_mix: Optional[float] = None) -> int:
         wid = C.c_int32()
@@ -194,6 +206,23 @@ class Device:
         self._check(self.lib.qiw_warp_train(self.h, wid, x.ctypes.data, w.ctypes.data, len(w), steps, batch, lr,
                                             C.byref(loss)))
         return loss.value
+
+    def warp_train_batch(self, wids: Sequence[int], xs: Sequence[np.ndarray], ws: Sequence[np.ndarray],
+                         steps: int = 400, batch: int = 4096, lr: float = 3e-3) -> np.ndarray:
+        """warp_train of several distinct warps at once (trained concurrently on the device);
+        returns their final losses."""
+        n = len(wids)
+        xs = [np.ascontiguousarray(x, dtype=np.float64) for x in xs]
+        ws = [np.ascontiguousarray(w, dtype=np.float64) for w in ws]
+        ids = np.ascontiguousarray(wids, dtype=np.int32)
+        xp = (C.c_void_p * n)(*[x.ctypes.data for x in xs])
+        wp = (C.c_void_p * n)(*[w.ctypes.data for w in ws])
+        cnt = np.ascontiguousarray([len(w) for w in ws], dtype=np.int64)
+        loss = np.zeros(n)
+        self._check(self.lib.qiw_warp_train_batch(self.h, n, ids.ctypes.data, C.cast(xp, C.c_void_p),
+                                                  C.cast(wp, C.c_void_p), cnt.ctypes.data, steps, batch, lr,
+                                                  loss.ctypes.data))
+        return loss
 
     def warp_map(self, wid: int, D: int, first: int, n: int, m=None, x0=None) -> np.ndarray:
         m = np.ascontiguousarray(self.sobol(D) if m is None else m, dtype=np.uint32)

@@ -346,15 +346,14 @@ def inchworm(expansion, orders, orders_bare, N_samples: int, n_pts_after_max: Op
         ses.dev.set_ppgf(expansion.P)
         if warp_policy is not None and n >= warp_policy.first_step and \
                 (n - warp_policy.first_step) % warp_policy.refit_every == 0:
-            from .warp import fit_group_warp
-            for td in top_bold:
-                if td.order == 0 or 2 * td.order > 8:
-                    continue
-                gid = ses.group(_lib.QIW_GROUP_BOLD, td)
-                fit = fit_group_warp(ses.dev, Work(gid, grid.tau(0), grid.tau(n), grid.tau(n + 1), 0, 0, 0),
-                                     n_train=warp_policy.n_train, steps=warp_policy.train_steps,
-                                     uniform_mix=warp_policy.uniform_mix, N_test=warp_policy.N_test,
-                                     R=warp_policy.R, min_gain=warp_policy.min_gain)
+            from .warp import fit_group_warps
+            gids = [ses.group(_lib.QIW_GROUP_BOLD, td) for td in top_bold if 0 < td.order and 2 * td.order <= 8]
+            fits = fit_group_warps(ses.dev, [Work(gid, grid.tau(0), grid.tau(n), grid.tau(n + 1), 0, 0, 0)
+                                             for gid in gids],
+                                   n_train=warp_policy.n_train, steps=warp_policy.train_steps,
+                                   uniform_mix=warp_policy.uniform_mix, N_test=warp_policy.N_test,
+                                   R=warp_policy.R, min_gain=warp_policy.min_gain)
+            for gid, fit in zip(gids, fits):
                 if fit.warp_id is None:
                     warps.pop(gid, None)
                 else:

@@ -118,3 +118,65 @@ def test_inchworm_with_warp_policy_is_unbiased(device):
     e_warp = err(solve(1024, WarpPolicy(refit_every=6, first_step=4, n_train=2 ** 14, R=8)))
     print(f"eg n_tau=24, N=1024: error plain {e_plain:.2e}, warped {e_warp:.2e}")
     assert np.isfinite(e_warp) and e_warp < 1.5 * e_plain
+
+
+def test_concurrent_training_equals_one_at_a_time(device):
+    """qiw_warp_train_batch trains distinct warps concurrently on several streams; each warp's
+    parameters and final loss equal those of training it alone (qiw_warp_train)."""
+    rng = np.random.default_rng(21)
+    data = []
+    for D in (2, 4, 6, 8, 4):
+        n = int(rng.integers(3000, 9000))
+        data.append((D, rng.random((n, D)), rng.random(n) + 0.01))
+    solo, solo_loss = [], []
+    for k, (D, X, w) in enumerate(data):
+        wid = device.warp_create(D, seed=30 + k)
+        solo_loss.append(device.warp_train(wid, X, w, steps=40, batch=1024, lr=3e-3))
+        solo.append(device.warp_params(wid))
+    wids = [device.warp_create(D, seed=30 + k) for k, (D, _, _) in enumerate(data)]
+    loss = device.warp_train_batch(wids, [X for (_, X, _) in data], [w for (_, _, w) in data], steps=40,
+                                   batch=1024, lr=3e-3)
+    for k, wid in enumerate(wids):
+        assert np.array_equal(device.warp_params(wid), solo[k]), k
+        assert loss[k] == solo_loss[k]
+
+
+def test_per_sample_values_of_several_items_in_one_launch(device):
+    """qiw_integrate_samples_batch returns each item's per-sample values, equal to one
+    qiw_integrate_samples call per item (batches of a sample are summed by atomics, so the
+    last bit may differ), and sums equal to the items' integrals."""
+    exp = models.eg_discrete_bath(n_tau=40)
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    g = exp.grid
+    works = []
+    for (o, npa, first, n) in ((1, 1, 0, 64), (2, 2, 5, 100), (3, 3, 1000, 37)):
+        gid = device.create_group(_lib.QIW_GROUP_BOLD, o, npa, get_topologies_at_order(o, npa))
+        works.append(Work(gid, g.tau(0), g.tau(20), g.tau(21), first, n, 4096))
+    blocks, samples = device.integrate_samples_batch(works, _lib.QIW_PREC_FP64)
+    for wk, b, s in zip(works, blocks, samples):
+        b1, s1 = device.integrate_samples(wk, _lib.QIW_PREC_FP64)
+        assert s.shape == s1.shape == (wk.n_samples, s1.shape[1])
+        assert np.allclose(s, s1, rtol=1e-13, atol=1e-13 * np.abs(s1).max())
+        for x, y in zip(b, b1):
+            assert np.allclose(x, y, rtol=1e-13, atol=1e-15)
+
+
+def test_fitting_groups_together_equals_one_at_a_time(device):
+    """fit_group_warps (one launch for all training samples, concurrent training, one launch per
+    estimator for the replicas) gives every group the gain and loss of fitting it alone."""
+    exp = models.eg_discrete_bath(n_tau=64)
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    g = exp.grid
+    t = (g.tau(0), g.tau(60), g.tau(61))
+    works = []
+    for (o, npa) in ((1, 1), (2, 1), (2, 2), (3, 3)):
+        gid = device.create_group(_lib.QIW_GROUP_BOLD, o, npa, get_topologies_at_order(o, npa))
+        works.append(Work(gid, *t, 0, 0, 0))
+    kw = dict(n_train=2 ** 12, steps=60, R=4, N_test=256)
+    together = qwarp.fit_group_warps(device, works, **kw)
+    for wk, f in zip(works, together):
+        alone = qwarp.fit_group_warp(device, wk, **kw)
+        assert np.isclose(f.gain, alone.gain, rtol=1e-6) and np.isclose(f.loss, alone.loss, rtol=1e-6)
+        assert (f.warp_id is None) == (alone.warp_id is None)
