@@ -781,31 +781,42 @@ int qiw_warp_train_batch(qiw_ctx *c, int32_t n_warps, const int32_t *ids, const 
       if ((rc = c->cuda(cudaStreamWaitEvent(c->aux[i], c->aux_ev[0], 0), "warp train: fork"))) return rc;
   }
   auto stream_of = [&](int k) { return n_st == 0 ? c->stream : c->aux[k % n_st]; };
-  const float b1 = 0.9f, b2 = 0.999f;
-  for (int s = 0; s < steps; ++s) {
-    for (int k = 0; k < n_warps; ++k) {
-      WarpRec *w = c->warps[ids[k]];
-      cudaStream_t st = stream_of(k);
-      const int64_t nb = std::max<int64_t>(1, n[k] / batch);
-      const int64_t lo = (s % nb) * batch, cnt = std::min<int64_t>(batch, n[k] - lo);
-      if ((rc = run_grad(c, w, w->X.p + lo * w->D, w->w.p + lo, cnt, st))) return rc;
-      w->t += 1;
-      const float c1 = 1.f - std::pow(b1, (float)w->t), c2 = 1.f - std::pow(b2, (float)w->t);
-      adam_kernel<<<64, 256, 0, st>>>(w->p.p, w->m.p, w->v.p, w->g.p, w->mask.p, w->wq.p, Layout(w->D).n, (float)lr,
-                                      b1, b2, 1e-8f, c1, c2);
-      if ((rc = c->cuda(cudaGetLastError(), "adam kernel"))) return rc;
+  auto enqueue = [&]() -> int {
+    const float b1 = 0.9f, b2 = 0.999f;
+    int r;
+    for (int s = 0; s < steps; ++s) {
+      for (int k = 0; k < n_warps; ++k) {
+        WarpRec *w = c->warps[ids[k]];
+        cudaStream_t st = stream_of(k);
+        const int64_t nb = std::max<int64_t>(1, n[k] / batch);
+        const int64_t lo = (s % nb) * batch, cnt = std::min<int64_t>(batch, n[k] - lo);
+        if ((r = run_grad(c, w, w->X.p + lo * w->D, w->w.p + lo, cnt, st))) return r;
+        w->t += 1;
+        const float c1 = 1.f - std::pow(b1, (float)w->t), c2 = 1.f - std::pow(b2, (float)w->t);
+        adam_kernel<<<64, 256, 0, st>>>(w->p.p, w->m.p, w->v.p, w->g.p, w->mask.p, w->wq.p, Layout(w->D).n,
+                                        (float)lr, b1, b2, 1e-8f, c1, c2);
+        if ((r = c->cuda(cudaGetLastError(), "adam kernel"))) return r;
+      }
+    }
+    if (final_loss)
+      for (int k = 0; k < n_warps; ++k) {
+        WarpRec *w = c->warps[ids[k]];
+        if ((r = run_grad(c, w, w->X.p, w->w.p, n[k], stream_of(k)))) return r;
+      }
+    return QIW_OK;
+  };
+  rc = enqueue();
+  // join the auxiliary streams back into the context stream, also after a failed launch, so
+  // later work on the context stream is ordered after everything enqueued here
+  for (int i = 0; i < n_st; ++i) {
+    int r2;
+    if ((r2 = c->cuda(cudaEventRecord(c->aux_ev[i], c->aux[i]), "warp train: join")) ||
+        (r2 = c->cuda(cudaStreamWaitEvent(c->stream, c->aux_ev[i], 0), "warp train: join"))) {
+      cudaStreamSynchronize(c->aux[i]);
+      if (!rc) rc = r2;
     }
   }
-  if (final_loss)
-    for (int k = 0; k < n_warps; ++k) {
-      WarpRec *w = c->warps[ids[k]];
-      if ((rc = run_grad(c, w, w->X.p, w->w.p, n[k], stream_of(k)))) return rc;
-    }
-  if (n_st > 0)
-    for (int i = 0; i < n_st; ++i)
-      if ((rc = c->cuda(cudaEventRecord(c->aux_ev[i], c->aux[i]), "warp train: join")) ||
-          (rc = c->cuda(cudaStreamWaitEvent(c->stream, c->aux_ev[i], 0), "warp train: join")))
-        return rc;
+  if (rc) return rc;
   if (final_loss) {
     std::vector<float> loss(n_warps, 0.f);
     for (int k = 0; k < n_warps; ++k)

@@ -180,3 +180,11 @@ def test_fitting_groups_together_equals_one_at_a_time(device):
         alone = qwarp.fit_group_warp(device, wk, **kw)
         assert np.isclose(f.gain, alone.gain, rtol=1e-6) and np.isclose(f.loss, alone.loss, rtol=1e-6)
         assert (f.warp_id is None) == (alone.warp_id is None)
+
+
+def test_training_the_same_warp_twice_at_once_is_rejected(device):
+    from qiw._lib import QiwError
+    wid = device.warp_create(4, seed=1)
+    X = np.random.default_rng(0).random((256, 4))
+    with pytest.raises(QiwError, match="twice"):
+        device.warp_train_batch([wid, wid], [X, X], [np.ones(256)] * 2, steps=2, batch=128)
