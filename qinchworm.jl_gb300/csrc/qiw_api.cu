@@ -119,7 +119,8 @@ int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
       (rc = c->cuda(c->d_partials.reserve((size_t)n_cta * t.res_max), "alloc partials")) ||
       (rc = c->cuda(c->d_out.reserve((size_t)2 * t.out_total), "alloc out")))
     return rc;
-  rc = launch_tables(c, t, precision, c->d_groups.p, c->d_works.p, c->d_cta_map.p, c->d_cta_first.p,
+  const DevGroup *dgroups = t.level > 0 ? c->d_groups_split[t.level - 1].p : c->d_groups.p;
+  rc = launch_tables(c, t, precision, dgroups, c->d_works.p, c->d_cta_map.p, c->d_cta_first.p,
                      c->d_res_sizes.p, c->d_out_off.p, c->d_partials.p, c->d_err.p, c->d_out.p);
   if (rc) return rc;
   int err_word = 0;
@@ -138,6 +139,31 @@ int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
   return QIW_OK;
 }
 
+// Split level of an FP32 launch.  A thread runs its batch's instructions one after another, and
+// at few waves of tiles the launch lasts as long as its longest batch; split-batch programs
+// shorten that at the price of more instructions in all.  Measured on the eg inch step (ms per
+// step, no split / 11000 / 9000 instructions per batch): 512 samples 13.6 / 10.9 / 9.7, 1024
+// 14.3 / 13.2 / 14.5, 4096 44.7 / 47.4 / 51.4.  So: under 1.5 waves level 2, under 4 level 1,
+// otherwise the plain programs.  QIW_SPLIT_LEVEL=0|1|2 fixes the level (tuning).
+static int split_level(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work) {
+  if (const char *e = std::getenv("QIW_SPLIT_LEVEL")) return std::max(0, std::min(kSplitLevels, std::atoi(e)));
+  if (c->n_sm <= 0) return 0;
+  bool any = false;
+  double tiles_x_threads = 0.0;   // samples in flight over the launch, tiles counted whole
+  for (int i = 0; i < n_work; ++i) {
+    const qiw_work_desc &wd = work[i];
+    if (wd.group < 0 || wd.group >= (int)c->groups.size()) return 0;   // rejected by the caller
+    const GroupRec &g = *c->groups[wd.group];
+    any = any || g.split[0] != nullptr;
+    const uint64_t n = g.plan.D == 0 ? 1 : wd.n_samples;
+    const double tiles = (double)((n + c->threads32 - 1) / c->threads32);
+    tiles_x_threads += tiles * c->threads32 * (double)(g.plan.batch_begin.size() - 1);
+  }
+  if (!any) return 0;
+  const double waves = tiles_x_threads / ((double)c->n_sm * kMinBlocks32 * kMaxThreads);
+  return waves < 1.5 ? 2 : waves < 4.0 ? 1 : 0;
+}
+
 int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, LaunchTables *t) {
   if (precision != QIW_PREC_FP64 && precision != QIW_PREC_FP32 && precision != QIW_PREC_FP32_TC)
     return c->fail(QIW_ERR_ARG, "qiw_integrate: unknown precision");
@@ -148,10 +174,11 @@ int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
   t->res_sizes.assign(n_work, 0);
   t->out_off.assign(n_work, 0);
   const int threads = precision == QIW_PREC_FP64 ? c->threads : c->threads32;  // samples per tile
+  t->level = precision == QIW_PREC_FP64 ? 0 : split_level(c, n_work, work);
   for (int i = 0; i < n_work; ++i) {
     const qiw_work_desc &wd = work[i];
     if (wd.group < 0 || wd.group >= (int)c->groups.size()) return c->fail(QIW_ERR_ARG, "qiw_integrate: bad group id");
-    const Plan &p = c->groups[wd.group]->plan;
+    const Plan &p = c->groups[wd.group]->level(t->level).plan;
     if (p.use_bold) need_P = true;
     if (p.D > 0 && (!wd.sobol_m || !wd.sobol_x0)) return c->fail(QIW_ERR_ARG, "qiw_integrate: Sobol tables missing");
     const bool no_tw = p.kind == QIW_GROUP_BARE || p.kind == QIW_GROUP_SIGMA;
@@ -241,6 +268,12 @@ int sync_groups(qiw_ctx *c) {
   for (auto *g : c->groups) dgs.push_back(g->dg);
   int rc = c->cuda(c->d_groups.upload(dgs.data(), dgs.size(), c->stream), "upload groups");
   if (rc) return rc;
+  for (int L = 1; L <= kSplitLevels; ++L) {
+    dgs.clear();
+    for (auto *g : c->groups) dgs.push_back(g->level(L).dg);
+    if ((rc = c->cuda(c->d_groups_split[L - 1].upload(dgs.data(), dgs.size(), c->stream), "upload groups")))
+      return rc;
+  }
   c->groups_dirty = false;
   return QIW_OK;
 }
@@ -332,8 +365,8 @@ void plan_store_insert(std::string &&key, const Plan &p) {
 }
 
 // Plans a group on c's problem (or takes the plan from c's cache), uploads its program and
-// fills its device descriptor.
-int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
+// fills its device descriptor.  max_instrs > 0: batches split to at most that many instructions.
+static int build_program(qiw_ctx *c, const GroupSpec &gs, int64_t max_instrs, GroupRec **out) {
   PlanOptions opt;
   opt.arena_budget = kArenaLarge;
   if (const char *b = std::getenv("QIW_ARENA_BUDGET")) opt.arena_budget = std::max<int64_t>(256, std::atoll(b));
@@ -341,9 +374,12 @@ int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
   // tuning: split batches whose per-sample work exceeds this many flops (a thread runs a batch
   // serially, so the heaviest batch bounds a launch's duration from below)
   if (const char *m = std::getenv("QIW_MAX_BATCH_FLOPS")) opt.max_batch_flops = std::max(0.0, std::atof(m));
+  if (const char *m = std::getenv("QIW_MAX_BATCH_INSTRS")) opt.max_batch_instrs = std::max<int64_t>(0, std::atoll(m));
+  if (max_instrs > 0) opt.max_batch_instrs = max_instrs;
   std::string key = plan_key(c->hp, gs);
   key.append(reinterpret_cast<const char *>(&opt.arena_budget), sizeof(opt.arena_budget));
   key.append(reinterpret_cast<const char *>(&opt.max_batch_flops), sizeof(opt.max_batch_flops));
+  key.append(reinterpret_cast<const char *>(&opt.max_batch_instrs), sizeof(opt.max_batch_instrs));
   GroupRec *g = new GroupRec();
   if (std::shared_ptr<const Plan> hit = plan_store_find(key)) {
     g->plan = *hit;
@@ -422,6 +458,30 @@ int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out) {
   return QIW_OK;
 }
 
+int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out, bool with_splits) {
+  GroupRec *g = nullptr;
+  int rc = build_program(c, gs, 0, &g);
+  if (rc) return rc;
+  // split-batch programs for FP32 launches of few waves: groups with small blocks (not the
+  // large-block or all-scalar programs) whose longest batch is above a level's instruction cap
+  if (with_splits && !g->dg.scalar && g->plan.arena <= kArenaLarge) {
+    int64_t longest = 0;
+    for (size_t b = 0; b + 1 < g->plan.batch_begin.size(); ++b)
+      longest = std::max<int64_t>(longest, g->plan.batch_begin[b + 1] - g->plan.batch_begin[b]);
+    for (int L = 0; L < kSplitLevels; ++L) {
+      if (longest <= kSplitInstrs[L]) continue;
+      GroupRec *sp = nullptr;
+      if (build_program(c, gs, kSplitInstrs[L], &sp) == QIW_OK) {
+        g->split[L] = sp;
+      } else {
+        c->err.clear();   // no split program for this level: launches use the plain one
+      }
+    }
+  }
+  *out = g;
+  return QIW_OK;
+}
+
 }  // namespace qiw
 
 extern "C" {
@@ -433,6 +493,7 @@ int qiw_ctx_create(qiw_ctx **out, int device) {
   if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return QIW_ERR_CUDA;
   qiw_ctx *c = new qiw_ctx();
   c->device = device;
+  if (cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) c->n_sm = 0;
   qiw::DeviceScope dev_scope(device);
   if (dev_scope.status != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
@@ -457,6 +518,7 @@ void qiw_ctx_destroy(qiw_ctx *c) {
   c->clear_groups();
   destroy_warps(c);
   c->d_groups.release();
+  for (auto &d : c->d_groups_split) d.release();
   c->d_pts.release();
   c->d_samples.release();
   for (auto *b : {&c->d_dims, &c->d_ptab_off, &c->d_eoff, &c->d_res_off, &c->d_delta_kind, &c->d_delta_off,
@@ -599,7 +661,7 @@ int qiw_group_create(qiw_ctx *c, const qiw_group_desc *d, int32_t *group_id) {
     if (grc) return c->fail(grc, "qiw_group_create: " + e);
   }
   GroupRec *g = nullptr;
-  int rc = build_group(c, gs, &g);
+  int rc = build_group(c, gs, &g, true);
   if (rc) return rc;
   c->groups.push_back(g);
   c->groups_dirty = true;

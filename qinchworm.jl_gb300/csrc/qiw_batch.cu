@@ -323,11 +323,7 @@ void qiw_batch_destroy(qiw_batch *b) {
     delete s;
   }
   for (PlanEntry &e : b->plans) {
-    e.rec->pm.release();
-    e.rec->wj.release();
-    e.rec->ins.release();
-    e.rec->ins32.release();
-    e.rec->batch.release();
+    e.rec->release();
     delete e.rec;
   }
   b->d_probs.release();

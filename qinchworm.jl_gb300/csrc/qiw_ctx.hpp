@@ -57,6 +57,12 @@ struct DeviceScope {
   DeviceScope &operator=(const DeviceScope &) = delete;
 };
 
+// FP32 launches of few waves are bound by the longest batch a thread runs (its instruction
+// count), not by throughput: a group may carry programs whose batches are split to at most
+// kSplitInstrs[L] instructions (topology halves; more instructions in all), chosen per launch.
+constexpr int kSplitLevels = 2;
+constexpr int64_t kSplitInstrs[kSplitLevels] = {11000, 9000};
+
 struct GroupRec {
   Plan plan;
   DevBuf<PmJob> pm;
@@ -64,6 +70,20 @@ struct GroupRec {
   DevBuf<Instr> ins, ins32;
   DevBuf<int32_t> batch;
   DevGroup dg;
+  GroupRec *split[kSplitLevels] = {nullptr, nullptr};   // split-batch programs (null: same as this one)
+  void release() {
+    pm.release();
+    wj.release();
+    ins.release();
+    ins32.release();
+    batch.release();
+    for (GroupRec *&s : split) {
+      if (s) s->release(), delete s;
+      s = nullptr;
+    }
+  }
+  // the program of split level L (0: this one)
+  const GroupRec &level(int L) const { return (L > 0 && split[L - 1]) ? *split[L - 1] : *this; }
 };
 
 struct WarpRec;
@@ -78,6 +98,7 @@ struct LaunchTables {
   std::vector<uint32_t> sobol;
   int64_t arena_max = 0;
   int res_max = 0, out_total = 0;
+  int level = 0;                      // split level of the programs the tables refer to
 };
 
 }  // namespace qiw
@@ -105,6 +126,8 @@ struct qiw_ctx {
 
   std::vector<qiw::GroupRec *> groups;
   qiw::DevBuf<qiw::DevGroup> d_groups;
+  qiw::DevBuf<qiw::DevGroup> d_groups_split[qiw::kSplitLevels];   // per split level (parallel to d_groups)
+  int n_sm = 0;                 // multiprocessors of the device
   bool groups_dirty = true;
 
   qiw::DevBuf<qiw::DevWork> d_works;
@@ -132,11 +155,7 @@ struct qiw_ctx {
   }
   void clear_groups() {
     for (auto *g : groups) {
-      g->pm.release();
-      g->wj.release();
-      g->ins.release();
-      g->ins32.release();
-      g->batch.release();
+      g->release();
       delete g;
     }
     groups.clear();
@@ -170,7 +189,8 @@ namespace qiw {
 // Validates the work items and builds the launch tables (no device memory touched).
 int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, LaunchTables *t);
 // Plans a group on c's problem, uploads its program and fills its device descriptor.
-int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out);
+// with_splits: also plan the split-batch programs of FP32 launches (kSplitInstrs).
+int build_group(qiw_ctx *c, const GroupSpec &gs, GroupRec **out, bool with_splits = false);
 // Uploads the group descriptor table if groups changed.
 int sync_groups(qiw_ctx *c);
 // Learned warps (csrc/qiw_warp.cu).

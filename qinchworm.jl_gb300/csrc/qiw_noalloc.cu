@@ -73,7 +73,7 @@ extern "C" int qiw_integrate_noalloc(qiw_ctx *c, int32_t n_work, const qiw_work_
   const int n_cta = (int)t.cta_map.size();
   // scratch layout: groups | works | cta_map | cta_first | res_sizes | out_off | sobol | err | partials
   std::vector<DevGroup> dgs;
-  for (auto *g : c->groups) dgs.push_back(g->dg);
+  for (auto *g : c->groups) dgs.push_back(g->level(t.level).dg);
   size_t o = 0;
   const size_t o_groups = o;    o = align256(o + sizeof(DevGroup) * dgs.size());
   const size_t o_works = o;     o = align256(o + sizeof(DevWork) * t.works.size());

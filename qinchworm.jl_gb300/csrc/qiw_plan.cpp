@@ -778,7 +778,8 @@ int plan_group(const HostProblem &pb, const GroupSpec &g, const PlanOptions &opt
     double fl = 0.0;
     r = B.schedule(nodes, edges, bi, &peak, &fl, res_off);
     if (r) return r;
-    const bool too_long = opt.max_batch_flops > 0.0 && fl > opt.max_batch_flops;   // one thread's serial work
+    const bool too_long = (opt.max_batch_flops > 0.0 && fl > opt.max_batch_flops) ||   // one thread's serial work
+                          (opt.max_batch_instrs > 0 && (int64_t)bi.size() > opt.max_batch_instrs);
     if ((peak > dyn_budget || too_long) && roots.size() > 1) {
       // split: by initial sector first, then by topology halves
       std::vector<std::pair<int, int>> a, b;

@@ -35,6 +35,7 @@ struct PlanOptions {
   bool fold_scalar_ops = true;   // fold 1x1 operator blocks into coefficients
   bool fuse_scalar = true;       // all sectors 1-dimensional: fuse a P multiply into its only AXPY
   double max_batch_flops = 0.0;  // > 0: split batches above this many flops per sample (topology halves)
+  int64_t max_batch_instrs = 0;  // > 0: split batches above this many instructions (topology halves)
 };
 
 struct Plan {

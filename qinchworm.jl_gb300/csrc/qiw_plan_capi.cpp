@@ -22,6 +22,8 @@ extern "C" int qiwp_plan(const qiw_problem_desc *pd, const qiw_group_desc *gd, i
   if (!rc) {
     PlanOptions opt;
     opt.arena_budget = arena_budget;
+    if (const char *m = std::getenv("QIW_MAX_BATCH_FLOPS")) opt.max_batch_flops = std::atof(m);
+    if (const char *m = std::getenv("QIW_MAX_BATCH_INSTRS")) opt.max_batch_instrs = std::atoll(m);
     rc = plan_group(hp, gs, opt, &p, &e);
   }
   if (rc) {
@@ -63,10 +65,33 @@ extern "C" int qiwp_batch_flops(const qiw_problem_desc *pd, const qiw_group_desc
     PlanOptions opt;
     opt.arena_budget = arena_budget;
     if (const char *m = std::getenv("QIW_MAX_BATCH_FLOPS")) opt.max_batch_flops = std::atof(m);
+    if (const char *m = std::getenv("QIW_MAX_BATCH_INSTRS")) opt.max_batch_instrs = std::atoll(m);
     rc = plan_group(hp, gs, opt, &p, &e);
   }
   if (rc) return -rc;
   const int n = (int)p.batch_flops.size();
   for (int i = 0; i < n && i < cap; ++i) out[i] = p.batch_flops[i];
+  return n;
+}
+
+// Instruction index where each batch of a planned group starts (n_batches + 1 entries).
+extern "C" int qiwp_batch_begin(const qiw_problem_desc *pd, const qiw_group_desc *gd, int64_t arena_budget,
+                                int32_t *out, int cap) {
+  std::string e;
+  HostProblem hp;
+  GroupSpec gs;
+  int rc = host_problem_from_desc(pd, &hp, &e);
+  if (!rc) rc = group_spec_from_desc(gd, &gs, &e);
+  Plan p;
+  if (!rc) {
+    PlanOptions opt;
+    opt.arena_budget = arena_budget;
+    if (const char *m = std::getenv("QIW_MAX_BATCH_FLOPS")) opt.max_batch_flops = std::atof(m);
+    if (const char *m = std::getenv("QIW_MAX_BATCH_INSTRS")) opt.max_batch_instrs = std::atoll(m);
+    rc = plan_group(hp, gs, opt, &p, &e);
+  }
+  if (rc) return -rc;
+  const int n = (int)p.batch_begin.size();
+  for (int i = 0; i < n && i < cap; ++i) out[i] = p.batch_begin[i];
   return n;
 }

@@ -85,6 +85,30 @@ def test_budget_split_gives_same_result():
     assert hp_b.arena <= budget < hp_a.arena
 
 
+def test_instruction_cap_split_gives_same_result(monkeypatch):
+    """Split-batch programs (batches capped at a number of instructions, the FP32 launches of
+    few waves) sum to the same result, with more batches and none above the cap."""
+    exp = models.eg_discrete_bath(n_tau=24)
+    g = exp.grid
+    t = (g.tau(0), g.tau(9), g.tau(10))
+    rel_a, hp_a = _case(exp, _lib.QIW_GROUP_BOLD, 4, 4, t, 4)
+    cap = 9000
+    monkeypatch.setenv("QIW_MAX_BATCH_INSTRS", str(cap))
+    rel_b, hp_b = _case(exp, _lib.QIW_GROUP_BOLD, 4, 4, t, 4)
+    assert rel_a < REL and rel_b < REL
+    assert hp_b.batches > hp_a.batches and len(hp_b.ins) > len(hp_a.ins)
+    import ctypes as C
+    lib = pe.plan_lib()
+    lib.qiwp_batch_begin.restype = C.c_int
+    pk = _lib.PackedProblem(exp)
+    gd, keep = _lib.pack_group(_lib.QIW_GROUP_BOLD, 4, 4, get_topologies_at_order(4, 4))
+    bb = np.zeros(1024, np.int32)
+    pd = pk.desc()
+    n = lib.qiwp_batch_begin(C.byref(pd), C.byref(gd), C.c_int64(8192), bb.ctypes.data_as(C.c_void_p), bb.size)
+    assert n == int(hp_b.batches) + 1 and bb[n - 1] == len(hp_b.ins)
+    assert np.diff(bb[:n]).max() <= cap
+
+
 def test_packing_limits_are_reported():
     """The planner packs positions and pair indices into bytes: a problem with more than 256
     interaction pairs is refused with QIW_ERR_UNSUPPORTED instead of being planned wrongly."""
