@@ -422,6 +422,7 @@ static int build_program(qiw_ctx *c, const GroupSpec &gs, int64_t max_instrs, Gr
       (rc = c->cuda(g->ins32.upload(ins32.data(), ins32.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(g->batch.upload(p.batch_begin.data(), p.batch_begin.size(), c->stream), "upload plan")) ||
       (rc = c->cuda(cudaStreamSynchronize(c->stream), "upload plan"))) {
+    g->release();
     delete g;
     return rc;
   }
