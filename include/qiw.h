@@ -210,6 +210,10 @@ int qiw_integrate_samples(qiw_ctx *ctx, const qiw_work_desc *work, int32_t preci
  * per-sample values one after another (item i: [n_samples_i][sum d_s^2]). */
 int qiw_integrate_samples_batch(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, int32_t precision,
                                 double *out, double *samples);
+/* The same with only the Euclidean norm of each sample's values returned (norms[sum n_samples_i],
+ * item after item): the training weights ||f_i|| of a learned warp, without copying the values. */
+int qiw_integrate_sample_norms(qiw_ctx *ctx, int32_t n_work, const qiw_work_desc *work, int32_t precision,
+                               double *out, double *norms);
 
 /* Kernel time of the most recent qiw_integrate (ms, CUDA events on the context stream). */
 double qiw_last_kernel_ms(const qiw_ctx *ctx);

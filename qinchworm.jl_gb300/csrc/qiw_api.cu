@@ -55,7 +55,7 @@ double simplex_volume(int d, double edge) {
 namespace qiw {
 
 int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, double *out,
-                   const int32_t *warp_ids, double *sample_out) {
+                   const int32_t *warp_ids, double *sample_out, double *norms_out) {
   if (!c || n_work < 0 || (n_work > 0 && (!work || !out))) return QIW_ERR_ARG;
   qiw::DeviceScope dev_scope(c->device);
   if (dev_scope.status != cudaSuccess) return c->cuda(dev_scope.status, "qiw_integrate: cudaSetDevice");
@@ -97,7 +97,7 @@ int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
   }
   // per-sample values: one region per work item, in work order
   size_t n_sample_vals = 0;
-  if (sample_out) {
+  if (sample_out || norms_out) {
     for (int i = 0; i < n_work; ++i) n_sample_vals += (size_t)t.works[i].n_samples * t.res_sizes[i];
     if ((rc = c->cuda(c->d_samples.reserve(n_sample_vals), "alloc samples")) ||
         (rc = c->cuda(cudaMemsetAsync(c->d_samples.p, 0, sizeof(double) * n_sample_vals, st), "clear samples")))
@@ -131,6 +131,23 @@ int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
       (rc = c->cuda(cudaMemcpyAsync(sample_out, c->d_samples.p, sizeof(double) * n_sample_vals,
                                     cudaMemcpyDeviceToHost, st), "copy samples")))
     return rc;
+  if (norms_out) {   // per-sample norms only: the values stay on the device
+    size_t n_rows = 0;
+    for (int i = 0; i < n_work; ++i) n_rows += (size_t)t.works[i].n_samples;
+    if ((rc = c->cuda(c->d_norms.reserve(n_rows), "alloc norms"))) return rc;
+    size_t o = 0, r = 0;
+    for (int i = 0; i < n_work; ++i) {
+      const uint64_t n = t.works[i].n_samples;
+      if ((rc = c->cuda(launch_row_norms(c->d_samples.p + o, n, t.res_sizes[i], c->d_norms.p + r, st), "norm kernel")))
+        return rc;
+      o += (size_t)n * t.res_sizes[i];
+      r += (size_t)n;
+    }
+    if (n_rows > 0 &&
+        (rc = c->cuda(cudaMemcpyAsync(norms_out, c->d_norms.p, sizeof(double) * n_rows, cudaMemcpyDeviceToHost, st),
+                      "copy norms")))
+      return rc;
+  }
   if ((rc = c->cuda(cudaStreamSynchronize(st), "integrate"))) return rc;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
@@ -522,6 +539,7 @@ void qiw_ctx_destroy(qiw_ctx *c) {
   for (auto &d : c->d_groups_split) d.release();
   c->d_pts.release();
   c->d_samples.release();
+  c->d_norms.release();
   for (auto *b : {&c->d_dims, &c->d_ptab_off, &c->d_eoff, &c->d_res_off, &c->d_delta_kind, &c->d_delta_off,
                   &c->d_cta_first, &c->d_res_sizes, &c->d_out_off, &c->d_err})
     b->release();
@@ -717,6 +735,12 @@ int qiw_integrate_samples_batch(qiw_ctx *c, int32_t n_work, const qiw_work_desc 
                                 double *out, double *samples) {
   if (!c || n_work < 0 || (n_work > 0 && (!work || !out || !samples))) return QIW_ERR_ARG;
   return integrate_impl(c, n_work, work, precision, out, nullptr, samples);
+}
+
+int qiw_integrate_sample_norms(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision,
+                               double *out, double *norms) {
+  if (!c || n_work < 0 || (n_work > 0 && (!work || !out || !norms))) return QIW_ERR_ARG;
+  return integrate_impl(c, n_work, work, precision, out, nullptr, nullptr, norms);
 }
 
 int qiw_sobol_points(qiw_ctx *c, int32_t D, const uint32_t *m, const uint32_t *x0, uint64_t first, uint64_t n,

@@ -135,7 +135,7 @@ struct qiw_ctx {
   qiw::DevBuf<double> d_partials, d_out;
   qiw::DevBuf<int> d_cta_first, d_res_sizes, d_out_off, d_err;
   qiw::DevBuf<uint32_t> d_sobol;
-  qiw::DevBuf<double> d_pts, d_samples;
+  qiw::DevBuf<double> d_pts, d_samples, d_norms;
   std::vector<qiw::WarpRec *> warps;
   std::vector<cudaStream_t> aux;   // streams of concurrent warp training (created on first use)
   std::vector<cudaEvent_t> aux_ev; // their fork / join events
@@ -200,7 +200,7 @@ int warp_map_device(qiw_ctx *c, int id, const uint32_t *m_dev, const uint32_t *x
                     double *pts_dev);
 // qiw_integrate with optional learned warps per work item and optional per-sample results.
 int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, double *out,
-                   const int32_t *warp_ids, double *sample_out);
+                   const int32_t *warp_ids, double *sample_out, double *norms_out = nullptr);
 // Launches the kernels on launch tables already in device memory (timed by ev0/ev1).
 int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const DevGroup *groups, const DevWork *works,
                   const int4 *cta_map, const int *cta_first, const int *res_sizes, const int *out_off,

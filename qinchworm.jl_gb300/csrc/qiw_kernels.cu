@@ -72,6 +72,23 @@ cudaError_t launch_sobol_points(const uint32_t *m, const uint32_t *x0, int D, ui
   return cudaGetLastError();
 }
 
+// Euclidean norm of each row of a [n][rs] array (per-sample values -> training weights): one
+// thread per row, the squares summed in row order.
+__global__ void row_norms_kernel(const double *__restrict__ v, uint64_t n, int rs, double *__restrict__ out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double *r = v + i * (uint64_t)rs;
+  double s = 0.0;
+  for (int e = 0; e < rs; ++e) s = fma(r[e], r[e], s);
+  out[i] = sqrt(s);
+}
+
+cudaError_t launch_row_norms(const double *v, uint64_t n, int rs, double *out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  row_norms_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(v, n, rs, out);
+  return cudaGetLastError();
+}
+
 template <typename T, int ARENA, int RESMAX>
 static cudaError_t launch_t(const LaunchArgs &a) {
   size_t smem = eval_smem_bytes(a.threads, RESMAX, a.stage) + (size_t)a.extra_smem;

@@ -107,6 +107,8 @@ cudaError_t launch_eval(const LaunchArgs &a);
 cudaError_t launch_eval_extras(const LaunchArgs &a);   // csrc/qiw_kernels_x.cu
 cudaError_t launch_finish(const FinishArgs &a);
 cudaError_t launch_fma_peak(bool fp32, void *out, int blocks, int threads, int iters, cudaStream_t st);
+// out[i] = || v[i][0 .. rs) ||_2 for i < n.
+cudaError_t launch_row_norms(const double *v, uint64_t n, int rs, double *out, cudaStream_t st);
 cudaError_t launch_sobol_points(const uint32_t *m, const uint32_t *x0, int D, uint64_t first, uint64_t n,
                                 uint32_t *out, cudaStream_t st);
 

@@ -40,7 +40,7 @@ EXPORTS = ["qiw_ctx_create", "qiw_ctx_destroy", "qiw_last_error", "qiw_problem_s
            "qiw_integrate_warped", "qiw_integrate_samples", "qiw_batch_create", "qiw_batch_destroy",
            "qiw_batch_last_error", "qiw_batch_add", "qiw_batch_run", "qiw_batch_get_P", "qiw_batch_stats_get",
            "qiw_plan_cache_info", "qiw_plan_cache_clear", "qiw_sobol_points", "qiw_warp_train_batch",
-           "qiw_integrate_samples_batch"]
+           "qiw_integrate_samples_batch", "qiw_integrate_sample_norms"]
 
 QIW_BATCH_GRAPH = 1
 QIW_BATCH_AUTOTUNE = 2
@@ -130,6 +130,8 @@ def load(path: Optional[str] = None) -> C.CDLL:
     lib.qiw_integrate_samples.argtypes = [C.c_void_p, C.POINTER(WorkDesc), C.c_int32, C.c_void_p, C.c_void_p]
     lib.qiw_integrate_samples_batch.argtypes = [C.c_void_p, C.c_int32, C.POINTER(WorkDesc), C.c_int32, C.c_void_p,
                                                 C.c_void_p]
+    lib.qiw_integrate_sample_norms.argtypes = [C.c_void_p, C.c_int32, C.POINTER(WorkDesc), C.c_int32, C.c_void_p,
+                                               C.c_void_p]
     lib.qiw_warp_train_batch.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_int32, C.c_int32, C.c_double, C.c_void_p]
     lib.qiw_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]

@@ -207,6 +207,18 @@ class Device:
                                             C.byref(loss)))
         return loss.value
 
+    def integrate_sample_norms(self, works: Sequence[Work], precision: int = _lib.QIW_PREC_FP64):
+        """integrate_samples_batch returning only each sample's value norm ||f_i||: (blocks per
+        item, norms per item [n_samples_i])."""
+        descs, keep = self._descs(works)
+        rs = int(np.sum(self.packed.dims ** 2))
+        out = np.zeros(2 * rs * len(works))
+        norms = np.zeros(sum(w.n_samples for w in works))
+        self._check(self.lib.qiw_integrate_sample_norms(self.h, len(works), descs, precision, out.ctypes.data,
+                                                        norms.ctypes.data))
+        cut = np.cumsum([0] + [w.n_samples for w in works])
+        return self._unpack(out, len(works)), [norms[a:b] for a, b in zip(cut[:-1], cut[1:])]
+
     def warp_train_batch(self, wids: Sequence[int], xs: Sequence[np.ndarray], ws: Sequence[np.ndarray],
                          steps: int = 400, batch: int = 4096, lr: float = 3e-3) -> np.ndarray:
         """warp_train of several distinct warps at once (trained concurrently on the device);

@@ -66,8 +66,8 @@ def fit_group_warps(dev: Device, works: Sequence[Work], n_train: int = 2 ** 15, 
                     min_gain: float = 1.0, precision: int = _lib.QIW_PREC_FP32) -> List[WarpFit]:
     """Train a warp for each work item's group at its inch times and decide whether to use it.
 
-    Training data are ``n_train`` plain Sobol samples of the group (their per-sample values
-    from qiw_integrate_samples, weight ||f||).  The decision compares the variances of R
+    Training data are ``n_train`` plain Sobol samples of the group (weight ||f|| of their
+    per-sample values, qiw_integrate_sample_norms).  The decision compares the variances of R
     scrambled replicas of N_test points each; the warp is kept when plain/warped > min_gain.
     The fit's own integrand evaluations run in ``precision`` (FP32 chains by default: the fit
     needs |f| and variance ratios, not 1e-12 values).  All groups share each step: one launch
@@ -83,11 +83,10 @@ def fit_group_warps(dev: Device, works: Sequence[Work], n_train: int = 2 ** 15, 
         else:
             live.append((i, work, D))
     if live:
-        _, samples = dev.integrate_samples_batch(
+        _, norms = dev.integrate_sample_norms(
             [Work(w.group, w.t_i, w.t_w, w.t_f, 0, n_train, n_train) for (_, w, _) in live], precision)
         train = []
-        for (i, work, D), smp in zip(live, samples):
-            w = np.linalg.norm(smp, axis=1)
+        for (i, work, D), w in zip(live, norms):
             if np.any(w > 0):
                 train.append((i, work, D, w))
             else:

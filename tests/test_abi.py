@@ -43,6 +43,7 @@ def test_null_arguments_are_rejected():
     assert lib.qiw_batch_run(None, 0, 0, None, 0) == _lib.QIW_ERR_ARG
     assert lib.qiw_batch_last_error(None) == b"null batch"
     assert lib.qiw_integrate_samples_batch(None, 1, None, 0, None, None) == _lib.QIW_ERR_ARG
+    assert lib.qiw_integrate_sample_norms(None, 1, None, 0, None, None) == _lib.QIW_ERR_ARG
     assert lib.qiw_warp_train_batch(None, 1, None, None, None, None, 10, 64, 1e-3, None) == _lib.QIW_ERR_ARG
 
 

@@ -402,3 +402,28 @@ def test_highest_orders_match_oracle(device, kind, order, npa):
     want = orc.OracleProblem(exp).integrate(_okind(kind), order, npa, [(x.pairs, x.parity) for x in tops], *t, N)
     assert _rel(device.integrate([Work(gid, *t, 0, N, N)])[0], want) < REL64
     assert _rel(device.integrate([Work(gid, *t, 0, N, N)], precision=_lib.QIW_PREC_FP32)[0], want) < REL32
+
+
+@pytest.mark.parametrize("npa", [4, 7])
+def test_fp32_split_batch_programs_match_oracle(device, monkeypatch, npa):
+    """eg order-4 groups carry split-batch programs (batches capped at 11000 / 9000
+    instructions) for FP32 launches of few waves; every level agrees with the oracle at the
+    FP32 tolerance, and the levels differ from each other by FP32 rounding only."""
+    exp = models.eg_discrete_bath(n_tau=40)
+    device.set_problem(exp)
+    device.set_ppgf(exp.P)
+    g = exp.grid
+    t = (g.tau(0), g.tau(20), g.tau(21))
+    tops = get_topologies_at_order(4, npa)
+    gid = device.create_group(_lib.QIW_GROUP_BOLD, 4, npa, tops)
+    N = 48
+    want = orc.OracleProblem(exp).integrate("bold", 4, npa, [(x.pairs, x.parity) for x in tops], *t, N)
+    got = {}
+    for level in (0, 1, 2):
+        monkeypatch.setenv("QIW_SPLIT_LEVEL", str(level))
+        got[level] = device.integrate([Work(gid, *t, 0, N, N)], _lib.QIW_PREC_FP32)[0]
+        assert _rel(got[level], want) < REL32, level
+    monkeypatch.delenv("QIW_SPLIT_LEVEL")
+    assert _rel(device.integrate([Work(gid, *t, 0, N, N)], _lib.QIW_PREC_FP32)[0], want) < REL32   # chosen level
+    for level in (1, 2):
+        assert _rel(got[level], got[0]) < 1e-5

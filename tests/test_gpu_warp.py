@@ -144,7 +144,8 @@ def test_concurrent_training_equals_one_at_a_time(device):
 def test_per_sample_values_of_several_items_in_one_launch(device):
     """qiw_integrate_samples_batch returns each item's per-sample values, equal to one
     qiw_integrate_samples call per item (batches of a sample are summed by atomics, so the
-    last bit may differ), and sums equal to the items' integrals."""
+    last bit may differ), and sums equal to the items' integrals; qiw_integrate_sample_norms
+    returns their norms."""
     exp = models.eg_discrete_bath(n_tau=40)
     device.set_problem(exp)
     device.set_ppgf(exp.P)
@@ -154,6 +155,9 @@ def test_per_sample_values_of_several_items_in_one_launch(device):
         gid = device.create_group(_lib.QIW_GROUP_BOLD, o, npa, get_topologies_at_order(o, npa))
         works.append(Work(gid, g.tau(0), g.tau(20), g.tau(21), first, n, 4096))
     blocks, samples = device.integrate_samples_batch(works, _lib.QIW_PREC_FP64)
+    _, norms = device.integrate_sample_norms(works, _lib.QIW_PREC_FP64)
+    for s, nr in zip(samples, norms):   # the training weights ||f_i||, computed on the device
+        assert np.allclose(nr, np.linalg.norm(s, axis=1), rtol=1e-14, atol=0)
     for wk, b, s in zip(works, blocks, samples):
         b1, s1 = device.integrate_samples(wk, _lib.QIW_PREC_FP64)
         assert s.shape == s1.shape == (wk.n_samples, s1.shape[1])
