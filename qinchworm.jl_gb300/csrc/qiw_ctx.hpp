@@ -78,7 +78,10 @@ struct GroupRec {
     ins32.release();
     batch.release();
     for (GroupRec *&s : split) {
-      if (s) s->release(), delete s;
+      if (s) {
+        s->release();
+        delete s;
+      }
       s = nullptr;
     }
   }
