@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "qiw_ctx.hpp"
+#include "qiw_dispatch.hpp"
 
 using namespace qiw;
 
@@ -423,14 +424,17 @@ static int build_program(qiw_ctx *c, const GroupSpec &gs, int64_t max_instrs, Gr
       I.flags = (uint8_t)((I.flags & ~3u) | (I.c != 1.0 ? 1 : 0) | (I.c == -1.0 ? 2 : 0));
     plan_store_insert(std::move(key), g->plan);
   }
-  // the FP32 copy holds c rounded to float in the low 4 bytes of c
+  // the FP32 copy holds c rounded to float in the low 4 bytes of c; each copy carries the flat
+  // dispatch index of the kernels that run it (FP32: P products held in registers)
   std::vector<Instr> ins32(g->plan.ins);
   for (Instr &I : ins32) {
     const float f = (float)I.c;
     uint64_t bits = 0;
     std::memcpy(&bits, &f, sizeof(f));
     std::memcpy(&I.c, &bits, sizeof(bits));
+    I.handler = QIW_FLAT_DISPATCH ? handler_of(I, QIW_REG_PRODUCTS) : 0;
   }
+  for (Instr &I : g->plan.ins) I.handler = QIW_FLAT_DISPATCH ? handler_of(I, QIW_REG_PRODUCTS && QIW_REG_PRODUCTS_FP64) : 0;
   const Plan &p = g->plan;
   int rc;
   if ((rc = c->cuda(g->pm.upload(p.pm.data(), p.pm.size(), c->stream), "upload plan")) ||

@@ -24,6 +24,7 @@
 #include <cstdint>
 
 #include "qiw.h"
+#include "qiw_dispatch.hpp"
 #include "qiw_internal.hpp"
 #include "qiw_kernels.hpp"
 
@@ -50,14 +51,8 @@ __device__ __forceinline__ Instr load_instr(const Instr *p) {
 // kRegTmp elements (dims 1, 2, 4).  Instruction flag bits set by the planner: 2 = the source is
 // the register copy, 3 = keep the product in registers, 4 = skip the product's arena store.
 constexpr int kRegTmp = 16;
-#ifndef QIW_REG_PRODUCTS
-#define QIW_REG_PRODUCTS 1
-#endif
 #ifndef QIW_BLOCK3
 #define QIW_BLOCK3 1
-#endif
-#ifndef QIW_REG_PRODUCTS_FP64
-#define QIW_REG_PRODUCTS_FP64 0
 #endif
 #ifndef QIW_PREFETCH_INSTR
 #define QIW_PREFETCH_INSTR 1
@@ -500,6 +495,75 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
   }
 }
 
+// Flat dispatch (Instr::handler, computed on upload by handler_of): one jump to the routine
+// instance for the instruction's opcode, block shape, coefficient mode and operand source.
+// REG: this kernel keeps P products in registers (the index was computed for such kernels).
+#define QIW_RC9(M, B) M(B + 0, 1, 1) M(B + 1, 1, 2) M(B + 2, 1, 4) M(B + 3, 2, 1) M(B + 4, 2, 2) \
+  M(B + 5, 2, 4) M(B + 6, 4, 1) M(B + 7, 4, 2) M(B + 8, 4, 4)
+#define QIW_RKC27(M, B) \
+  M(B + 0, 1, 1, 1) M(B + 1, 1, 1, 2) M(B + 2, 1, 1, 4) M(B + 3, 1, 2, 1) M(B + 4, 1, 2, 2) M(B + 5, 1, 2, 4) \
+  M(B + 6, 1, 4, 1) M(B + 7, 1, 4, 2) M(B + 8, 1, 4, 4) M(B + 9, 2, 1, 1) M(B + 10, 2, 1, 2) M(B + 11, 2, 1, 4) \
+  M(B + 12, 2, 2, 1) M(B + 13, 2, 2, 2) M(B + 14, 2, 2, 4) M(B + 15, 2, 4, 1) M(B + 16, 2, 4, 2) M(B + 17, 2, 4, 4) \
+  M(B + 18, 4, 1, 1) M(B + 19, 4, 1, 2) M(B + 20, 4, 1, 4) M(B + 21, 4, 2, 1) M(B + 22, 4, 2, 2) M(B + 23, 4, 2, 4) \
+  M(B + 24, 4, 4, 1) M(B + 25, 4, 4, 2) M(B + 26, 4, 4, 4)
+
+template <typename T, bool REG>
+__device__ __forceinline__ void exec_flat(const Instr &I, T *A, const T *O, T (&t)[kRegTmp]) {
+  const bool accf = I.acc != 0;
+  switch (I.handler) {
+#define QIW_H_PMULR(H, R, C) \
+  case H:                    \
+    if constexpr (REG) pmul_r<T, R, C>(A, t, I.dst, I.a, I.src, (I.flags & 16u) == 0); \
+    break;
+#define QIW_H_PMUL(H, R, C) \
+  case H:                   \
+    pmul_u<T, R, C>(A, I.dst, I.a, I.src); \
+    break;
+#define QIW_H_PMULD(H, R, C) \
+  case H:                    \
+    pmuld_u<T, R, C>(A, I.dst, I.a, I.src); \
+    break;
+#define QIW_H_OMUL(H, R, K, C, MODE, XR) \
+  case H:                                 \
+    if constexpr (REG || !XR)             \
+      omul_m<T, R, K, C, MODE, XR>(A, O, I.dst, I.a, I.src, MODE ? edge_coef<T>(I, A) : (T)1, accf, t); \
+    break;
+#define QIW_H_OMULRC(H, R, K, C) QIW_H_OMUL(H, R, K, C, 1, true)
+#define QIW_H_OMULR1(H, R, K, C) QIW_H_OMUL(H, R, K, C, 0, true)
+#define QIW_H_OMULC(H, R, K, C) QIW_H_OMUL(H, R, K, C, 1, false)
+#define QIW_H_OMUL1(H, R, K, C) QIW_H_OMUL(H, R, K, C, 0, false)
+    QIW_RC9(QIW_H_PMULR, kHPmulReg)
+    QIW_RC9(QIW_H_PMUL, kHPmul)
+    QIW_RC9(QIW_H_PMULD, kHPmulD)
+    QIW_RKC27(QIW_H_OMULRC, kHOmulRegC)
+    QIW_RKC27(QIW_H_OMULR1, kHOmulReg1)
+    QIW_RKC27(QIW_H_OMULC, kHOmulC)
+    QIW_RKC27(QIW_H_OMUL1, kHOmul1)
+#undef QIW_H_PMULR
+#undef QIW_H_PMUL
+#undef QIW_H_PMULD
+#undef QIW_H_OMUL
+#undef QIW_H_OMULRC
+#undef QIW_H_OMULR1
+#undef QIW_H_OMULC
+#undef QIW_H_OMUL1
+#define QIW_H_AXPY(H, N, XR)                                                                  \
+  case H:                                                                                     \
+    if constexpr (REG || !XR) axpy_u<T, N, XR>(A, I.dst, I.src, edge_coef<T>(I, A), accf,    \
+                                               (I.w >= 0) || has_c(I), t);                     \
+    break;
+    QIW_H_AXPY(kHAxpyReg + 0, 1, true) QIW_H_AXPY(kHAxpyReg + 1, 2, true) QIW_H_AXPY(kHAxpyReg + 2, 4, true)
+    QIW_H_AXPY(kHAxpyReg + 3, 8, true) QIW_H_AXPY(kHAxpyReg + 4, 16, true)
+    QIW_H_AXPY(kHAxpy + 0, 1, false) QIW_H_AXPY(kHAxpy + 1, 2, false) QIW_H_AXPY(kHAxpy + 2, 4, false)
+    QIW_H_AXPY(kHAxpy + 3, 8, false) QIW_H_AXPY(kHAxpy + 4, 16, false)
+#undef QIW_H_AXPY
+    default:
+      break;
+  }
+}
+#undef QIW_RC9
+#undef QIW_RKC27
+
 // LARGE: the instantiation for problems with large sector blocks (the largest arena class, e.g.
 // t2g's 9 x 9 blocks), whose products take the 3-row register blocking; the others keep products
 // of dims 1, 2, 4 in registers.  Both only in the FP32 kernels: the FP64 kernels are DFMA-bound
@@ -510,6 +574,12 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
                                            float *tcx) {
   constexpr bool REG = QIW_REG_PRODUCTS && (sizeof(T) == 4 || QIW_REG_PRODUCTS_FP64) && !LARGE;
   constexpr bool BLOCK3 = QIW_BLOCK3 && sizeof(T) == 4 && LARGE;
+  if constexpr (QIW_FLAT_DISPATCH && !LARGE) {
+    if (I.handler) {
+      exec_flat<T, REG>(I, A, O, t);
+      return;
+    }
+  }
   const int rows = I.rows, cols = I.cols;
   switch (I.op) {
     case OP_LOADP: {  // c == 1 copies (x * 1 is exact)

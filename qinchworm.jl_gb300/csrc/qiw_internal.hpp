@@ -27,7 +27,8 @@ struct alignas(16) Instr {     // 32 bytes
   uint8_t op, rows, inner, cols;
   uint8_t acc;                 // 1: accumulate into dst, 0: overwrite
   uint8_t flags;               // bit 0: c != 1, bit 1: c == -1 (set on upload; the kernels test no doubles)
-  uint8_t pad1, pad2;
+  uint8_t handler;             // flat dispatch index of the kernels (0: decode the fields), set on upload
+  uint8_t pad2;
   int32_t dst;                 // arena offset (elements)
   int32_t src;                 // arena offset (elements)
   int32_t a;                   // Pm offset (arena) / operator value offset / result offset
