@@ -497,7 +497,8 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
 
 // Flat dispatch (Instr::handler, computed on upload by handler_of): one jump to the routine
 // instance for the instruction's opcode, block shape, coefficient mode and operand source.
-// REG: this kernel keeps P products in registers (the index was computed for such kernels).
+// REG: this kernel keeps P products in registers; kernels that do not (FP64, large-block) run
+// the register-source entries through the arena, as they ignore flag bits 2-4 everywhere.
 #define QIW_RC9(M, B) M(B + 0, 1, 1) M(B + 1, 1, 2) M(B + 2, 1, 4) M(B + 3, 2, 1) M(B + 4, 2, 2) \
   M(B + 5, 2, 4) M(B + 6, 4, 1) M(B + 7, 4, 2) M(B + 8, 4, 4)
 #define QIW_RKC27(M, B) \
@@ -514,6 +515,7 @@ __device__ __forceinline__ void exec_flat(const Instr &I, T *A, const T *O, T (&
 #define QIW_H_PMULR(H, R, C) \
   case H:                    \
     if constexpr (REG) pmul_r<T, R, C>(A, t, I.dst, I.a, I.src, (I.flags & 16u) == 0); \
+    else pmul_u<T, R, C>(A, I.dst, I.a, I.src); \
     break;
 #define QIW_H_PMUL(H, R, C) \
   case H:                   \
@@ -525,8 +527,7 @@ __device__ __forceinline__ void exec_flat(const Instr &I, T *A, const T *O, T (&
     break;
 #define QIW_H_OMUL(H, R, K, C, MODE, XR) \
   case H:                                 \
-    if constexpr (REG || !XR)             \
-      omul_m<T, R, K, C, MODE, XR>(A, O, I.dst, I.a, I.src, MODE ? edge_coef<T>(I, A) : (T)1, accf, t); \
+    omul_m<T, R, K, C, MODE, XR && REG>(A, O, I.dst, I.a, I.src, MODE ? edge_coef<T>(I, A) : (T)1, accf, t); \
     break;
 #define QIW_H_OMULRC(H, R, K, C) QIW_H_OMUL(H, R, K, C, 1, true)
 #define QIW_H_OMULR1(H, R, K, C) QIW_H_OMUL(H, R, K, C, 0, true)
@@ -547,10 +548,9 @@ __device__ __forceinline__ void exec_flat(const Instr &I, T *A, const T *O, T (&
 #undef QIW_H_OMULR1
 #undef QIW_H_OMULC
 #undef QIW_H_OMUL1
-#define QIW_H_AXPY(H, N, XR)                                                                  \
-  case H:                                                                                     \
-    if constexpr (REG || !XR) axpy_u<T, N, XR>(A, I.dst, I.src, edge_coef<T>(I, A), accf,    \
-                                               (I.w >= 0) || has_c(I), t);                     \
+#define QIW_H_AXPY(H, N, XR)                                                                   \
+  case H:                                                                                      \
+    axpy_u<T, N, XR && REG>(A, I.dst, I.src, edge_coef<T>(I, A), accf, (I.w >= 0) || has_c(I), t); \
     break;
     QIW_H_AXPY(kHAxpyReg + 0, 1, true) QIW_H_AXPY(kHAxpyReg + 1, 2, true) QIW_H_AXPY(kHAxpyReg + 2, 4, true)
     QIW_H_AXPY(kHAxpyReg + 3, 8, true) QIW_H_AXPY(kHAxpyReg + 4, 16, true)
@@ -574,12 +574,13 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
                                            float *tcx) {
   constexpr bool REG = QIW_REG_PRODUCTS && (sizeof(T) == 4 || QIW_REG_PRODUCTS_FP64) && !LARGE;
   constexpr bool BLOCK3 = QIW_BLOCK3 && sizeof(T) == 4 && LARGE;
-  if constexpr (QIW_FLAT_DISPATCH && !LARGE) {
-    if (I.handler) {
+  if constexpr (QIW_FLAT_DISPATCH) {
+    if (I.handler) {   // blocks of dims 1, 2, 4: the decoded cases below are the rest
       exec_flat<T, REG>(I, A, O, t);
       return;
     }
   }
+  constexpr bool DECODE_SMALL = !QIW_FLAT_DISPATCH;   // the small-block cases, when not dispatched flat
   const int rows = I.rows, cols = I.cols;
   switch (I.op) {
     case OP_LOADP: {  // c == 1 copies (x * 1 is exact)
@@ -614,13 +615,17 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
     }
     case OP_PMUL: {
       const int cr = dcode(rows), cc = dcode(cols);
-      if (REG && (I.flags & 8u)) {   // dims 1, 2, 4 by construction (planner)
-        const int code = cr * 3 + cc;
-        const bool store = (I.flags & 16u) == 0;
-        QIW_D2(pmul_r, A, t, I.dst, I.a, I.src, store)
-      } else if (cr >= 0 && cc >= 0) {
-        const int code = cr * 3 + cc;
-        QIW_D2(pmul_u, A, I.dst, I.a, I.src)
+      if (DECODE_SMALL && REG && (I.flags & 8u)) {   // dims 1, 2, 4 by construction (planner)
+        if constexpr (DECODE_SMALL) {
+          const int code = cr * 3 + cc;
+          const bool store = (I.flags & 16u) == 0;
+          QIW_D2(pmul_r, A, t, I.dst, I.a, I.src, store)
+        }
+      } else if (DECODE_SMALL && cr >= 0 && cc >= 0) {
+        if constexpr (DECODE_SMALL) {
+          const int code = cr * 3 + cc;
+          QIW_D2(pmul_u, A, I.dst, I.a, I.src)
+        }
       } else if (BLOCK3 && rows % 3 == 0 && rows <= 9) {
         mul_rows3<T, false>(A, O, I.dst, I.a, I.src, rows, rows, cols, (T)1, false, false);
       } else {
@@ -638,9 +643,11 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
     }
     case OP_PMULD: {
       const int cr = dcode(rows), cc = dcode(cols);
-      if (cr >= 0 && cc >= 0) {
-        const int code = cr * 3 + cc;
-        QIW_D2(pmuld_u, A, I.dst, I.a, I.src)
+      if (DECODE_SMALL && cr >= 0 && cc >= 0) {
+        if constexpr (DECODE_SMALL) {
+          const int code = cr * 3 + cc;
+          QIW_D2(pmuld_u, A, I.dst, I.a, I.src)
+        }
       } else {
 #pragma unroll 1
         for (int j = 0; j < cols; ++j)
@@ -654,12 +661,16 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
       const bool has_coef = (I.w >= 0) || has_c(I);
       const T coef = edge_coef<T>(I, A);
       const int cr = dcode(rows), ck = dcode(inner), cc = dcode(cols);
-      if (REG && (I.flags & 4u)) {   // source in registers: dims 1, 2, 4 by construction (planner)
-        const int code = cr * 9 + ck * 3 + cc;
-        QIW_D3(omul_ur, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef, t)
-      } else if (cr >= 0 && ck >= 0 && cc >= 0) {
-        const int code = cr * 9 + ck * 3 + cc;
-        QIW_D3(omul_u, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef, t)
+      if (DECODE_SMALL && REG && (I.flags & 4u)) {   // source in registers: dims 1, 2, 4 by construction (planner)
+        if constexpr (DECODE_SMALL) {
+          const int code = cr * 9 + ck * 3 + cc;
+          QIW_D3(omul_ur, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef, t)
+        }
+      } else if (DECODE_SMALL && cr >= 0 && ck >= 0 && cc >= 0) {
+        if constexpr (DECODE_SMALL) {
+          const int code = cr * 9 + ck * 3 + cc;
+          QIW_D3(omul_u, A, O, I.dst, I.a, I.src, coef, I.acc != 0, has_coef, t)
+        }
       } else if (BLOCK3 && tcx && inner == kTcK && rows <= 16 && cols <= kTcMaxCols) {
         if constexpr (BLOCK3) omul_tc(A, O, tcx, I.dst, I.a, I.src, rows, cols, coef, I.acc != 0);
       } else if (BLOCK3 && rows % 3 == 0 && inner <= 9 && !(I.acc && I.dst == I.src)) {
@@ -683,8 +694,8 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
       const T coef = edge_coef<T>(I, A);
       const int n = rows * cols;
       const bool accf = I.acc != 0;
-      if (REG && (I.flags & 4u)) {   // source in registers (n in 1, 2, 4, 8, 16 by construction)
-        switch (n) {
+      if (DECODE_SMALL && REG && (I.flags & 4u)) {   // source in registers (n in 1, 2, 4, 8, 16 by construction)
+        if constexpr (DECODE_SMALL) switch (n) {
           case 1: axpy_u<T, 1, true>(A, I.dst, I.src, coef, accf, has_coef, t); break;
           case 2: axpy_u<T, 2, true>(A, I.dst, I.src, coef, accf, has_coef, t); break;
           case 4: axpy_u<T, 4, true>(A, I.dst, I.src, coef, accf, has_coef, t); break;
@@ -693,18 +704,26 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
         }
         break;
       }
-      switch (n) {
-        case 1: axpy_u<T, 1, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
-        case 2: axpy_u<T, 2, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
-        case 4: axpy_u<T, 4, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
-        case 8: axpy_u<T, 8, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
-        case 16: axpy_u<T, 16, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
-        default:
+      if constexpr (DECODE_SMALL) {
+        switch (n) {
+          case 1: axpy_u<T, 1, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+          case 2: axpy_u<T, 2, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+          case 4: axpy_u<T, 4, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+          case 8: axpy_u<T, 8, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+          case 16: axpy_u<T, 16, false>(A, I.dst, I.src, coef, accf, has_coef, t); break;
+          default:
 #pragma unroll 1
-          for (int e = 0; e < n; ++e) {
-            const int o = I.dst + e;
-            A[o] = accf ? fmaT<T>(coef, A[I.src + e], A[o]) : coef * A[I.src + e];
-          }
+            for (int e = 0; e < n; ++e) {
+              const int o = I.dst + e;
+              A[o] = accf ? fmaT<T>(coef, A[I.src + e], A[o]) : coef * A[I.src + e];
+            }
+        }
+      } else {   // sizes other than 1, 2, 4, 8, 16 (the others are dispatched flat)
+#pragma unroll 1
+        for (int e = 0; e < n; ++e) {
+          const int o = I.dst + e;
+          A[o] = accf ? fmaT<T>(coef, A[I.src + e], A[o]) : coef * A[I.src + e];
+        }
       }
       break;
     }
