@@ -86,14 +86,23 @@ int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
     }
     if (total > 0) {
       if ((rc = c->cuda(c->d_pts.reserve(total), "alloc warped points"))) return rc;
+      // the maps of different items are independent: several run concurrently on auxiliary
+      // streams (each a few CTAs), joined back before the evaluation launch
+      int n_warped = 0;
+      for (int i = 0; i < n_work; ++i) n_warped += warp_ids[i] >= 0 && t.works[i].n_samples > 0;
+      const int n_st = n_warped > 1 ? std::min(n_warped, kAuxStreams) : 0;
+      if (n_st > 0 && ((rc = aux_streams(c, n_st)) || (rc = aux_fork(c, n_st)))) return rc;
+      int k = 0;
       for (int i = 0; i < n_work; ++i) {
         if (warp_ids[i] < 0) continue;
         double *dst = c->d_pts.p + poff[i];
         if ((rc = warp_map_device(c, warp_ids[i], t.works[i].m, t.works[i].x0, t.works[i].first_index,
-                                  t.works[i].n_samples, dst)))
-          return rc;
+                                  t.works[i].n_samples, dst, n_st > 0 ? c->aux[k++ % n_st] : nullptr)))
+          break;
         t.works[i].pts = dst;
       }
+      const int rj = n_st > 0 ? aux_join(c, n_st) : QIW_OK;
+      if (rc || (rc = rj)) return rc;
     }
   }
   // per-sample values: one region per work item, in work order

@@ -200,7 +200,12 @@ int sync_groups(qiw_ctx *c);
 void destroy_warps(qiw_ctx *c);
 int warp_dim(qiw_ctx *c, int id);
 int warp_map_device(qiw_ctx *c, int id, const uint32_t *m_dev, const uint32_t *x0_dev, uint64_t first, uint64_t n,
-                    double *pts_dev);
+                    double *pts_dev, cudaStream_t st = nullptr);   // st null: the context stream
+// Auxiliary streams of a context: create up to n, fork them from the context stream (they wait
+// for its work so far), join them back (the context stream waits for theirs).
+int aux_streams(qiw_ctx *c, int n);
+int aux_fork(qiw_ctx *c, int n);
+int aux_join(qiw_ctx *c, int n);
 // qiw_integrate with optional learned warps per work item and optional per-sample results.
 int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_t precision, double *out,
                    const int32_t *warp_ids, double *sample_out, double *norms_out = nullptr);

@@ -549,8 +549,46 @@ int warp_dim(qiw_ctx *c, int id) { return c->warps[id]->D; }
     default: CALL(8); break;       \
   }
 
+int aux_streams(qiw_ctx *c, int n) {
+  int rc;
+  for (int i = (int)c->aux.size(); i < n; ++i) {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev = nullptr;
+    if ((rc = c->cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "auxiliary streams"))) return rc;
+    if ((rc = c->cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "auxiliary streams"))) {
+      cudaStreamDestroy(s);
+      return rc;
+    }
+    c->aux.push_back(s);
+    c->aux_ev.push_back(ev);
+  }
+  return QIW_OK;
+}
+
+int aux_fork(qiw_ctx *c, int n) {
+  int rc;
+  if ((rc = c->cuda(cudaEventRecord(c->aux_ev[0], c->stream), "auxiliary streams: fork"))) return rc;
+  for (int i = 0; i < n; ++i)
+    if ((rc = c->cuda(cudaStreamWaitEvent(c->aux[i], c->aux_ev[0], 0), "auxiliary streams: fork"))) return rc;
+  return QIW_OK;
+}
+
+int aux_join(qiw_ctx *c, int n) {
+  int rc = QIW_OK;
+  for (int i = 0; i < n; ++i) {
+    int r2;
+    if ((r2 = c->cuda(cudaEventRecord(c->aux_ev[i], c->aux[i]), "auxiliary streams: join")) ||
+        (r2 = c->cuda(cudaStreamWaitEvent(c->stream, c->aux_ev[i], 0), "auxiliary streams: join"))) {
+      cudaStreamSynchronize(c->aux[i]);
+      if (!rc) rc = r2;
+    }
+  }
+  return rc;
+}
+
 int warp_map_device(qiw_ctx *c, int id, const uint32_t *m_dev, const uint32_t *x0_dev, uint64_t first, uint64_t n,
-                    double *pts_dev) {
+                    double *pts_dev, cudaStream_t st) {
+  if (!st) st = c->stream;
   WarpRec *w = c->warps[id];
   const unsigned blocks = (unsigned)((n + WTILE - 1) / WTILE);
   if (blocks == 0) return QIW_OK;
@@ -560,7 +598,7 @@ int warp_map_device(qiw_ctx *c, int id, const uint32_t *m_dev, const uint32_t *x
     const size_t smem = tc_map_smem<DD>();                                                                 \
     e = cudaFuncSetAttribute(warp_map_tc_kernel<DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
     if (e == cudaSuccess)                                                                                  \
-      warp_map_tc_kernel<DD><<<blocks, 128, smem, c->stream>>>(w->wq.p, w->alpha, m_dev, x0_dev, first, n, pts_dev); \
+      warp_map_tc_kernel<DD><<<blocks, 128, smem, st>>>(w->wq.p, w->alpha, m_dev, x0_dev, first, n, pts_dev); \
   }
   QIW_WARP_D_SWITCH(w->D, QIW_MAP_CALL)
 #undef QIW_MAP_CALL
@@ -764,22 +802,7 @@ int qiw_warp_train_batch(qiw_ctx *c, int32_t n_warps, const int32_t *ids, const 
   // the context stream.  Each warp owns its parameters, moments and gradient rows, so the
   // results are those of training the warps one after another.
   const int n_st = n_warps == 1 ? 0 : std::min(n_warps, kAuxStreams);
-  for (int i = (int)c->aux.size(); i < n_st; ++i) {
-    cudaStream_t s = nullptr;
-    cudaEvent_t ev = nullptr;
-    if ((rc = c->cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "warp train: streams"))) return rc;
-    if ((rc = c->cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "warp train: streams"))) {
-      cudaStreamDestroy(s);
-      return rc;
-    }
-    c->aux.push_back(s);
-    c->aux_ev.push_back(ev);
-  }
-  if (n_st > 0) {
-    if ((rc = c->cuda(cudaEventRecord(c->aux_ev[0], c->stream), "warp train: fork"))) return rc;
-    for (int i = 0; i < n_st; ++i)
-      if ((rc = c->cuda(cudaStreamWaitEvent(c->aux[i], c->aux_ev[0], 0), "warp train: fork"))) return rc;
-  }
+  if (n_st > 0 && ((rc = aux_streams(c, n_st)) || (rc = aux_fork(c, n_st)))) return rc;
   auto stream_of = [&](int k) { return n_st == 0 ? c->stream : c->aux[k % n_st]; };
   auto enqueue = [&]() -> int {
     const float b1 = 0.9f, b2 = 0.999f;
@@ -808,15 +831,8 @@ int qiw_warp_train_batch(qiw_ctx *c, int32_t n_warps, const int32_t *ids, const 
   rc = enqueue();
   // join the auxiliary streams back into the context stream, also after a failed launch, so
   // later work on the context stream is ordered after everything enqueued here
-  for (int i = 0; i < n_st; ++i) {
-    int r2;
-    if ((r2 = c->cuda(cudaEventRecord(c->aux_ev[i], c->aux[i]), "warp train: join")) ||
-        (r2 = c->cuda(cudaStreamWaitEvent(c->stream, c->aux_ev[i], 0), "warp train: join"))) {
-      cudaStreamSynchronize(c->aux[i]);
-      if (!rc) rc = r2;
-    }
-  }
-  if (rc) return rc;
+  const int rj = aux_join(c, n_st);
+  if (rc || (rc = rj)) return rc;
   if (final_loss) {
     std::vector<float> loss(n_warps, 0.f);
     for (int k = 0; k < n_warps; ++k)
