@@ -57,6 +57,9 @@ constexpr int kRegTmp = 16;
 #ifndef QIW_PREFETCH_INSTR
 #define QIW_PREFETCH_INSTR 1
 #endif
+#ifndef QIW_SCALAR_SPLIT
+#define QIW_SCALAR_SPLIT 1
+#endif
 
 // Dynamic shared memory of the evaluation kernels: the reduction rows [warps][RESMAX] doubles,
 // then (launches with scalar programs) two instruction chunks of blockDim.x entries.
@@ -183,22 +186,25 @@ __device__ __forceinline__ void omul_m(T *A, const T *O, int dst, int oa, int sr
 #pragma unroll
     for (int i = 0; i < K * C; ++i) x[i] *= coef;
   }
+  // One body for both accumulation modes: the chain starts from the destination's value, or from
+  // zero when overwriting (fma(a, b, 0) is the rounded product a*b, so the roundings are those of
+  // a chain that starts with a multiply; only the sign of an exact zero can differ).
 #pragma unroll
   for (int j = 0; j < C; ++j)
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int d = dst + j * R + r;
+      const T base = accf ? A[d] : (T)0;
       T acc;
-      if (accf && !(MODE == 1 && !scale_src)) {
-        // accumulate into the destination: the chain starts from its value (K FMAs)
-        acc = A[d];
+      if constexpr (MODE == 1 && !scale_src) {   // coef * (O x), added to the destination
+        T sum = o[r] * x[j * K];
+#pragma unroll
+        for (int k = 1; k < K; ++k) sum = fmaT<T>(o[k * R + r], x[j * K + k], sum);
+        acc = fmaT<T>(coef, sum, base);
+      } else {                                    // the chain starts from the destination
+        acc = base;
 #pragma unroll
         for (int k = 0; k < K; ++k) acc = fmaT<T>(o[k * R + r], x[j * K + k], acc);
-      } else {
-        acc = o[r] * x[j * K];
-#pragma unroll
-        for (int k = 1; k < K; ++k) acc = fmaT<T>(o[k * R + r], x[j * K + k], acc);
-        if (MODE == 1 && !scale_src) acc = accf ? fmaT<T>(coef, acc, A[d]) : coef * acc;
       }
       A[d] = acc;
     }
@@ -226,12 +232,12 @@ __device__ __forceinline__ void axpy_u(T *A, int dst, int src, T coef, bool accf
   T x[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) x[i] = XR ? t[i] : A[src + i];
-  if (has_coef) {
+  if (has_coef) {   // fma(coef, x, 0) = coef * x
 #pragma unroll
-    for (int i = 0; i < N; ++i) A[dst + i] = accf ? fmaT<T>(coef, x[i], A[dst + i]) : coef * x[i];
+    for (int i = 0; i < N; ++i) A[dst + i] = fmaT<T>(coef, x[i], accf ? A[dst + i] : (T)0);
   } else {
 #pragma unroll
-    for (int i = 0; i < N; ++i) A[dst + i] = accf ? x[i] + A[dst + i] : x[i];
+    for (int i = 0; i < N; ++i) A[dst + i] = x[i] + (accf ? A[dst + i] : (T)0);
   }
 }
 
@@ -456,6 +462,7 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
     case OP_PMULD:
       A[I.dst] = A[I.a] * A[I.src];
       break;
+#if QIW_SCALAR_SPLIT
     case OP_OMUL: {  // the roundings of omul_m<T, 1, 1, 1, MODE>
       const T o = __ldg(O + I.a), x = A[I.src];
       if (I.w < 0 && !has_c(I)) {
@@ -487,6 +494,40 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
       }
       break;
     }
+#else
+    // the destination's value, or zero when overwriting (fma(a, b, 0) = a * b, x + 0 = x)
+    case OP_OMUL: {  // the roundings of omul_m<T, 1, 1, 1, MODE>
+      const T o = __ldg(O + I.a), x = A[I.src];
+      const T base = I.acc ? A[I.dst] : (T)0;
+      if (I.w < 0 && !has_c(I)) {
+        A[I.dst] = fmaT<T>(o, x, base);
+      } else {
+        const T coef = edge_coef<T>(I, A);
+        A[I.dst] = fmaT<T>(coef, o * x, base);
+      }
+      break;
+    }
+    case OP_AXPY: {  // the roundings of axpy_u<T, 1>
+      const T x = A[I.src];
+      const T base = I.acc ? A[I.dst] : (T)0;
+      if (I.w < 0 && !has_c(I)) {
+        A[I.dst] = x + base;
+      } else {
+        A[I.dst] = fmaT<T>(edge_coef<T>(I, A), x, base);
+      }
+      break;
+    }
+    case OP_PMAXPY: {  // PMUL then AXPY, the same roundings
+      const T x = A[I.a] * A[I.src];
+      const T base = I.acc ? A[I.dst] : (T)0;
+      if (I.w < 0 && !has_c(I)) {
+        A[I.dst] = x + base;
+      } else {
+        A[I.dst] = fmaT<T>(edge_coef<T>(I, A), x, base);
+      }
+      break;
+    }
+#endif
     case OP_LEAF:
       R[I.a] += (double)A[I.src];
       break;
