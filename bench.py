@@ -362,10 +362,10 @@ def run_reference(args):
 
 # DRAM bytes (read + write) of one eval_kernel launch of the default FP64 eg inch step, from one
 # ncu capture of `python bench.py --steps 2 --warmup 3 --no-cpu-baseline --no-parity
-# --no-time-to-tol` (dram__bytes_read.sum 22.80 GB + dram__bytes_write.sum 27.60 GB at 1024
+# --no-time-to-tol` (dram__bytes_read.sum 22.88 GB + dram__bytes_write.sum 27.65 GB at 1024
 # samples, one pass): the per-thread arenas spilling from L2.  It grows with the samples; other
 # workloads report null.
-EG_FP64_TRAFFIC_PER_1024 = 50.40e9
+EG_FP64_TRAFFIC_PER_1024 = 50.53e9
 
 
 def _traffic(args):

@@ -57,9 +57,6 @@ constexpr int kRegTmp = 16;
 #ifndef QIW_PREFETCH_INSTR
 #define QIW_PREFETCH_INSTR 1
 #endif
-#ifndef QIW_SCALAR_SPLIT
-#define QIW_SCALAR_SPLIT 1
-#endif
 
 // Dynamic shared memory of the evaluation kernels: the reduction rows [warps][RESMAX] doubles,
 // then (launches with scalar programs) two instruction chunks of blockDim.x entries.
@@ -462,7 +459,6 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
     case OP_PMULD:
       A[I.dst] = A[I.a] * A[I.src];
       break;
-#if QIW_SCALAR_SPLIT
     case OP_OMUL: {  // the roundings of omul_m<T, 1, 1, 1, MODE>
       const T o = __ldg(O + I.a), x = A[I.src];
       if (I.w < 0 && !has_c(I)) {
@@ -494,40 +490,6 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
       }
       break;
     }
-#else
-    // the destination's value, or zero when overwriting (fma(a, b, 0) = a * b, x + 0 = x)
-    case OP_OMUL: {  // the roundings of omul_m<T, 1, 1, 1, MODE>
-      const T o = __ldg(O + I.a), x = A[I.src];
-      const T base = I.acc ? A[I.dst] : (T)0;
-      if (I.w < 0 && !has_c(I)) {
-        A[I.dst] = fmaT<T>(o, x, base);
-      } else {
-        const T coef = edge_coef<T>(I, A);
-        A[I.dst] = fmaT<T>(coef, o * x, base);
-      }
-      break;
-    }
-    case OP_AXPY: {  // the roundings of axpy_u<T, 1>
-      const T x = A[I.src];
-      const T base = I.acc ? A[I.dst] : (T)0;
-      if (I.w < 0 && !has_c(I)) {
-        A[I.dst] = x + base;
-      } else {
-        A[I.dst] = fmaT<T>(edge_coef<T>(I, A), x, base);
-      }
-      break;
-    }
-    case OP_PMAXPY: {  // PMUL then AXPY, the same roundings
-      const T x = A[I.a] * A[I.src];
-      const T base = I.acc ? A[I.dst] : (T)0;
-      if (I.w < 0 && !has_c(I)) {
-        A[I.dst] = x + base;
-      } else {
-        A[I.dst] = fmaT<T>(edge_coef<T>(I, A), x, base);
-      }
-      break;
-    }
-#endif
     case OP_LEAF:
       R[I.a] += (double)A[I.src];
       break;
