@@ -16,7 +16,7 @@ INCLUDE = os.path.join(REPO, "include")
 
 SOURCES = ["qiw_kernels.cu", "qiw_kernels_x.cu", "qiw_batch_kernels.cu", "qiw_api.cu", "qiw_noalloc.cu",
            "qiw_warp.cu", "qiw_batch.cu", "qiw_plan.cpp"]
-HEADERS = ["qiw_internal.hpp", "qiw_kernels.hpp", "qiw_plan.hpp", "qiw_ctx.hpp", "qiw_eval.cuh"]
+HEADERS = ["qiw_internal.hpp", "qiw_kernels.hpp", "qiw_plan.hpp", "qiw_ctx.hpp", "qiw_eval.cuh", "qiw_dispatch.hpp"]
 PLAN_LIB = os.path.join(BUILD, "libqiw_plan_host.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
