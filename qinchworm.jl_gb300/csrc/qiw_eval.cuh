@@ -687,7 +687,7 @@ __device__ __forceinline__ void exec_instr(const Instr &I, T *A, const T *O, dou
 #pragma unroll 4
             for (int k = 0; k < inner; ++k) acc = fmaT<T>(__ldg(O + I.a + k * rows + r), A[I.src + j * inner + k], acc);
             const int o = I.dst + j * rows + r;
-            A[o] = I.acc ? fmaT<T>(coef, acc, A[o]) : coef * acc;
+            A[o] = fmaT<T>(coef, acc, I.acc ? A[o] : (T)0);   // fma(c, a, 0) = c * a
           }
       }
       break;
