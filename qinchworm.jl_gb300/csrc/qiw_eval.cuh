@@ -432,10 +432,19 @@ __device__ __forceinline__ bool has_c(const Instr &I) { return (I.flags & 1u) !=
 
 // Coefficient of an edge: c (flag bit 0: c != 1) times the per-sample weight A[w] when w >= 0.
 // c == -1 exactly (flag bit 1) is a sign flip, which the consuming FMA takes for free.
-template <typename T>
+// EAGER (block routines): the weight is loaded unconditionally (arena slot 0 always exists), so
+// the load issues with the instruction's other operand loads (FP32 eg step -4 %); the scalar
+// executor loads it only when the edge has one (its programs are bound by arena loads).
+template <typename T, bool EAGER = true>
 __device__ __forceinline__ T edge_coef(const Instr &I, const T *A) {
-  if (I.w < 0) return coef_c<T>(I);
-  const T w = A[I.w];
+  T w;
+  if constexpr (EAGER) {
+    w = A[I.w < 0 ? 0 : I.w];
+    if (I.w < 0) return coef_c<T>(I);
+  } else {
+    if (I.w < 0) return coef_c<T>(I);
+    w = A[I.w];
+  }
   if (!has_c(I)) return w;
   return (I.flags & 2u) ? -w : coef_c<T>(I) * w;
 }
@@ -464,7 +473,7 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
       if (I.w < 0 && !has_c(I)) {
         A[I.dst] = I.acc ? fmaT<T>(o, x, A[I.dst]) : o * x;
       } else {
-        const T coef = edge_coef<T>(I, A);
+        const T coef = edge_coef<T, false>(I, A);
         const T p = o * x;
         A[I.dst] = I.acc ? fmaT<T>(coef, p, A[I.dst]) : coef * p;
       }
@@ -475,7 +484,7 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
       if (I.w < 0 && !has_c(I)) {
         A[I.dst] = I.acc ? x + A[I.dst] : x;
       } else {
-        const T coef = edge_coef<T>(I, A);
+        const T coef = edge_coef<T, false>(I, A);
         A[I.dst] = I.acc ? fmaT<T>(coef, x, A[I.dst]) : coef * x;
       }
       break;
@@ -485,7 +494,7 @@ __device__ __forceinline__ void exec_scalar(const Instr &I, T *A, const T *O, do
       if (I.w < 0 && !has_c(I)) {
         A[I.dst] = I.acc ? x + A[I.dst] : x;
       } else {
-        const T coef = edge_coef<T>(I, A);
+        const T coef = edge_coef<T, false>(I, A);
         A[I.dst] = I.acc ? fmaT<T>(coef, x, A[I.dst]) : coef * x;
       }
       break;
