@@ -34,6 +34,11 @@ constexpr int kHOmul1 = 109;      // + rkc (27): the same without coefficient
 constexpr int kHAxpyReg = 136;    // + log2(n) (5): axpy, source in registers
 constexpr int kHAxpy = 141;       // + log2(n) (5): axpy, source in the arena
 constexpr int kHandlers = 146;
+static_assert(kHPmul == kHPmulReg + 9 && kHPmulD == kHPmul + 9 && kHOmulRegC == kHPmulD + 9 &&
+                  kHOmulReg1 == kHOmulRegC + 27 && kHOmulC == kHOmulReg1 + 27 && kHOmul1 == kHOmulC + 27 &&
+                  kHAxpyReg == kHOmul1 + 27 && kHAxpy == kHAxpyReg + 5 && kHandlers == kHAxpy + 5,
+              "dispatch ranges are contiguous and disjoint");
+static_assert(kHandlers <= 256, "the dispatch index is one byte");
 
 inline int small_code(int d) { return d == 1 ? 0 : d == 2 ? 1 : d == 4 ? 2 : -1; }
 inline int pow2_code(int n) { return n == 1 ? 0 : n == 2 ? 1 : n == 4 ? 2 : n == 8 ? 3 : n == 16 ? 4 : -1; }
