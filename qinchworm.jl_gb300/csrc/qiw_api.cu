@@ -172,8 +172,9 @@ int integrate_impl(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
 // step, no split / 11000 / 9000 instructions per batch): 512 samples 13.6 / 10.9 / 9.7, 1024
 // 14.3 / 13.2 / 14.5, 4096 44.7 / 47.4 / 51.4.  So: under 1.5 waves level 2, under 4 level 1,
 // otherwise the plain programs.  QIW_SPLIT_LEVEL=0|1|2 fixes the level (tuning).
-static int split_level(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work) {
-  if (const char *e = std::getenv("QIW_SPLIT_LEVEL")) return std::max(0, std::min(kSplitLevels, std::atoi(e)));
+// *waves: the launch's tiles x threads over the SMs' resident threads (plain programs).
+static int split_level(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, double *waves_out) {
+  *waves_out = 0.0;
   if (c->n_sm <= 0) return 0;
   bool any = false;
   double tiles_x_threads = 0.0;   // samples in flight over the launch, tiles counted whole
@@ -186,8 +187,10 @@ static int split_level(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work) {
     const double tiles = (double)((n + c->threads32 - 1) / c->threads32);
     tiles_x_threads += tiles * c->threads32 * (double)(g.plan.batch_begin.size() - 1);
   }
-  if (!any) return 0;
   const double waves = tiles_x_threads / ((double)c->n_sm * kMinBlocks32 * kMaxThreads);
+  *waves_out = waves;
+  if (const char *e = std::getenv("QIW_SPLIT_LEVEL")) return std::max(0, std::min(kSplitLevels, std::atoi(e)));
+  if (!any) return 0;
   return waves < 1.5 ? 2 : waves < 4.0 ? 1 : 0;
 }
 
@@ -201,7 +204,7 @@ int prepare_launch(qiw_ctx *c, int32_t n_work, const qiw_work_desc *work, int32_
   t->res_sizes.assign(n_work, 0);
   t->out_off.assign(n_work, 0);
   const int threads = precision == QIW_PREC_FP64 ? c->threads : c->threads32;  // samples per tile
-  t->level = precision == QIW_PREC_FP64 ? 0 : split_level(c, n_work, work);
+  t->level = precision == QIW_PREC_FP64 ? 0 : split_level(c, n_work, work, &t->waves);
   for (int i = 0; i < n_work; ++i) {
     const qiw_work_desc &wd = work[i];
     if (wd.group < 0 || wd.group >= (int)c->groups.size()) return c->fail(QIW_ERR_ARG, "qiw_integrate: bad group id");
@@ -324,6 +327,11 @@ int launch_tables(qiw_ctx *c, const LaunchTables &t, int32_t precision, const De
   la.res_max = t.res_max;
   la.fp32 = precision != QIW_PREC_FP64;
   la.tc_omul = precision == QIW_PREC_FP32_TC;
+  // FP32 launches of many waves are throughput-bound: kernels with more resident blocks (eg at
+  // 4096 samples 39.4 -> 34.1 ms, t2g 196.0 -> 186.8 ms); launches of few waves are bound by a
+  // thread's path and keep the 5-block kernels (the denser ones were 2-3 % slower there)
+  la.dense = la.fp32 && t.level == 0 && t.waves >= 4.0;
+  if (const char *e = std::getenv("QIW_DENSE")) la.dense = la.fp32 && std::atoi(e) != 0;
   la.extras = false;
   la.stage = false;
   for (const DevWork &w : t.works) {

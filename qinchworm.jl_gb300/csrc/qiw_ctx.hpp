@@ -102,6 +102,7 @@ struct LaunchTables {
   int64_t arena_max = 0;
   int res_max = 0, out_total = 0;
   int level = 0;                      // split level of the programs the tables refer to
+  double waves = 0.0;                 // FP32: tiles x threads over the SMs' resident threads
 };
 
 }  // namespace qiw

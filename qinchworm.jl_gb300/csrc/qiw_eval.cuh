@@ -1016,8 +1016,9 @@ __device__ __forceinline__ void eval_tile(const DevProblem &pb, const DevGroup &
   }
 }
 
-template <typename T, int ARENA, int RESMAX, bool EXTRAS>
-__global__ void __launch_bounds__(kMaxThreads, sizeof(T) == 4 ? kMinBlocks32 : kMinBlocks)
+// MINB: resident 128-thread blocks per SM the registers are sized for (the launch bound).
+template <typename T, int ARENA, int RESMAX, bool EXTRAS, int MINB = (sizeof(T) == 4 ? kMinBlocks32 : kMinBlocks)>
+__global__ void __launch_bounds__(kMaxThreads, MINB)
     eval_kernel(DevProblem pb, const DevGroup *__restrict__ groups, const DevWork *__restrict__ works,
                 const int4 *__restrict__ cta_map, double *__restrict__ partials) {
   const int4 cm = cta_map[blockIdx.x];   // (work item, batch, first sample of the tile, partial row)

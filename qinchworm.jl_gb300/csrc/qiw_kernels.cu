@@ -89,7 +89,7 @@ cudaError_t launch_row_norms(const double *v, uint64_t n, int rs, double *out, c
   return cudaGetLastError();
 }
 
-template <typename T, int ARENA, int RESMAX>
+template <typename T, int ARENA, int RESMAX, int MINB = (sizeof(T) == 4 ? kMinBlocks32 : kMinBlocks)>
 static cudaError_t launch_t(const LaunchArgs &a) {
   size_t smem = eval_smem_bytes(a.threads, RESMAX, a.stage) + (size_t)a.extra_smem;
   DevProblem pb = a.pb;
@@ -99,7 +99,7 @@ static cudaError_t launch_t(const LaunchArgs &a) {
     pb.tc_stage = (int32_t)smem;
     smem += (size_t)((a.threads + 31) / 32) * kTcWarpFloats * sizeof(float);
   }
-  auto *k = eval_kernel<T, ARENA, RESMAX, false>;
+  auto *k = eval_kernel<T, ARENA, RESMAX, false, MINB>;
   cudaError_t e;
   if (smem > (48u << 10) && (e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
     return e;
@@ -122,7 +122,12 @@ cudaError_t launch_eval(const LaunchArgs &a) {
   const int ac = arena_class(a.arena_max);
   if (a.fp32) {
     if (ac == 0) return big_res ? launch_t<float, kArenaSmall, kResLarge>(a) : launch_t<float, kArenaSmall, kResSmall>(a);
-    if (ac == 2) return launch_t<float, kArenaHuge, kResLarge>(a);
+    if (ac == 2)
+      return a.dense ? launch_t<float, kArenaHuge, kResLarge, kMinBlocks32DenseHuge>(a)
+                     : launch_t<float, kArenaHuge, kResLarge>(a);
+    if (a.dense)
+      return big_res ? launch_t<float, kArenaLarge, kResLarge, kMinBlocks32Dense>(a)
+                     : launch_t<float, kArenaLarge, kResSmall, kMinBlocks32Dense>(a);
     return big_res ? launch_t<float, kArenaLarge, kResLarge>(a) : launch_t<float, kArenaLarge, kResSmall>(a);
   }
   if (ac == 0) return big_res ? launch_t<double, kArenaSmall, kResLarge>(a) : launch_t<double, kArenaSmall, kResSmall>(a);

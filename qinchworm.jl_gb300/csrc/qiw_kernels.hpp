@@ -17,6 +17,10 @@ constexpr int kMinBlocks = QIW_MIN_BLOCKS;  // 128-thread blocks per SM: FP64 at
 #define QIW_MIN_BLOCKS_FP32 5
 #endif
 constexpr int kMinBlocks32 = QIW_MIN_BLOCKS_FP32;  // the same bound for the FP32 kernels
+// FP32 launches of many waves (throughput-bound) use kernels compiled for more resident blocks:
+// small-block programs 7 per SM (72 registers), large-block programs 6 (80 registers).
+constexpr int kMinBlocks32Dense = 7;
+constexpr int kMinBlocks32DenseHuge = 6;
 constexpr int kArenaSmall = 1024;    // per-sample arena instantiations (elements)
 constexpr int kArenaLarge = 8192;
 constexpr int kArenaHuge = 20480;   // large-sector problems (9x9 blocks); results always kResLarge
@@ -38,6 +42,7 @@ struct LaunchArgs {
   int extra_smem = 0;        // extra dynamic shared memory per CTA (occupancy tuning)
   bool tc_omul = false;      // FP32: operator multiplies of 9-wide blocks on tensor cores (large-block kernels)
   int carveout = -1;         // preferred shared-memory carveout, percent (-1: driver default)
+  bool dense = false;        // FP32, many waves of tiles: the kernels with more resident blocks
   cudaStream_t stream;
 };
 
