@@ -1,6 +1,7 @@
 """Host-side result handling of qiw.device.Device, without a GPU: the C library is replaced by a
 stand-in that writes a deterministic result buffer, so the unpacking, the packed layout and
-the correlator's trace extraction are checked against each other."""
+the correlator's trace extraction are checked against each other; and the call sequence and
+keep/drop decisions of fitting several groups' warps together, on a stand-in device."""
 import ctypes as C
 
 import numpy as np
@@ -106,3 +107,58 @@ def _positive_integrate(rs):
             buf[2 * k + 1] = -(1e-3 + k * 1e-6)
         return _lib.QIW_OK
     return f
+
+
+class _FitDevice:
+    """Stand-in for qiw.device.Device in fit_group_warps: deterministic per-sample norms and
+    replica results (the warped replicas of group 3 vary less than its plain ones, those of
+    group 2 more), and a record of the calls."""
+
+    def __init__(self):
+        self.group_info = {0: (1, 0, 0), 1: (1, 1, 1), 2: (1, 2, 2), 3: (1, 2, 3), 4: (1, 1, 1)}
+        self.calls = []
+        self.next_wid = 100
+
+    def integrate_sample_norms(self, works, precision):
+        self.calls.append(("norms", [w.group for w in works], [w.n_samples for w in works]))
+        norms = [np.zeros(w.n_samples) if w.group == 4 else np.linspace(1.0, 2.0, w.n_samples) for w in works]
+        return None, norms
+
+    def warp_create(self, D, seed=0, uniform_mix=None):
+        self.calls.append(("create", D, seed, uniform_mix))
+        self.next_wid += 1
+        return self.next_wid
+
+    def warp_train_batch(self, wids, xs, ws, steps, batch, lr):
+        self.calls.append(("train", list(wids), [x.shape for x in xs], [len(w) for w in ws], steps, batch))
+        return np.arange(len(wids), dtype=float) * 0.1
+
+    def integrate(self, works, precision, warps=None):
+        self.calls.append(("integrate", [w.group for w in works], warps is not None))
+        out = []
+        for k, w in enumerate(works):
+            r = k % 4   # replica index within the group (R = 4 below)
+            spread = {2: 1.0 if warps is None else 3.0, 3: 1.0 if warps is None else 0.2}.get(w.group, 1.0)
+            out.append([np.array([[1.0 + spread * (r - 1.5)]])])
+        return out
+
+
+def test_fit_group_warps_orchestration_without_a_gpu():
+    """fit_group_warps: order-0 groups and groups whose samples are all zero get no warp; the
+    others share one norms launch, one concurrent training call and one launch per estimator,
+    and keep their warp only where the warped replicas vary less (gain above min_gain = 1)."""
+    from qiw import warp as qwarp
+    dev = _FitDevice()
+    works = [Work(g, 0.0, 0.5, 1.0, 0, 0, 0) for g in (0, 1, 2, 3, 4)]
+    fits = qwarp.fit_group_warps(dev, works, n_train=256, steps=7, batch=64, R=4, N_test=32)
+    assert [f.warp_id is None for f in fits] == [True, True, True, False, True]
+    assert fits[0].gain == 1.0 and fits[4].gain == 1.0 and np.isclose(fits[1].gain, 1.0)
+    assert np.isclose(fits[2].gain, 1 / 9) and np.isclose(fits[3].gain, 25.0)
+    kinds = [c[0] for c in dev.calls]
+    assert kinds == ["norms", "create", "create", "create", "train", "integrate", "integrate"]
+    assert dev.calls[0][1] == [1, 2, 3, 4] and dev.calls[0][2] == [256] * 4
+    train = dev.calls[4]
+    assert train[2] == [(256, 2), (256, 4), (256, 4)] and train[3] == [256] * 3 and train[4:] == (7, 64)
+    assert dev.calls[5] == ("integrate", [1] * 4 + [2] * 4 + [3] * 4, False)
+    assert dev.calls[6] == ("integrate", [1] * 4 + [2] * 4 + [3] * 4, True)
+    assert [f.loss for f in fits] == [0.0, 0.0, 0.1, 0.2, 0.0]
