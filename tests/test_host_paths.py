@@ -20,6 +20,22 @@ class _FakeLib:
             buf[k] = k * 1e-3 if k % 2 == 0 else float((k // 2) % 7)
         return _lib.QIW_OK
 
+    def qiw_integrate_sample_norms(self, h, n, descs, precision, out, norms):
+        self.qiw_integrate(h, n, descs, precision, out)
+        total = sum(descs[i].n_samples for i in range(n))
+        buf = (C.c_double * total).from_address(norms)
+        for k in range(total):
+            buf[k] = float(k)
+        return _lib.QIW_OK
+
+    def qiw_integrate_samples_batch(self, h, n, descs, precision, out, samples):
+        self.qiw_integrate(h, n, descs, precision, out)
+        total = sum(descs[i].n_samples for i in range(n)) * self.rs
+        buf = (C.c_double * total).from_address(samples)
+        for k in range(total):
+            buf[k] = float(k)
+        return _lib.QIW_OK
+
     def qiw_problem_set(self, h, d):
         return _lib.QIW_OK
 
@@ -162,3 +178,17 @@ def test_fit_group_warps_orchestration_without_a_gpu():
     assert dev.calls[5] == ("integrate", [1] * 4 + [2] * 4 + [3] * 4, False)
     assert dev.calls[6] == ("integrate", [1] * 4 + [2] * 4 + [3] * 4, True)
     assert [f.loss for f in fits] == [0.0, 0.0, 0.1, 0.2, 0.0]
+
+
+def test_per_sample_results_are_split_by_work_item():
+    """integrate_sample_norms and integrate_samples_batch hand back one array per work item, in
+    work order, cut by the items' sample counts."""
+    exp = models.eg_discrete_bath(n_tau=8)
+    dev = _device(exp)
+    works = [Work(0, 0.0, 0.1, 0.2, 0, n, 64) for n in (5, 1, 7)]
+    _, norms = dev.integrate_sample_norms(works)
+    assert [list(x) for x in norms] == [[0, 1, 2, 3, 4], [5], [6, 7, 8, 9, 10, 11, 12]]
+    rs = dev.lib.rs
+    _, samples = dev.integrate_samples_batch(works)
+    assert [x.shape for x in samples] == [(5, rs), (1, rs), (7, rs)]
+    assert samples[1][0, 0] == 5 * rs and samples[2][-1, -1] == 13 * rs - 1
